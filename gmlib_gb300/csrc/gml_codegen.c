@@ -1,0 +1,319 @@
+/*
+ * gml_codegen.c -- CUDA C++ generation for GmlCompileKernel.
+ *
+ * Input: the argument table built by GmlCompileKernel (same construction as
+ * the reference, sources/gmlib3.c:2292-2499) and the user's OpenCL-C body.
+ * Output: one CUDA kernel source with the reference's naming contract, so the
+ * body compiles unchanged:
+ *
+ *   parameters   <nam>Tab per argument, in argument order, then
+ *                GmlParSct *GmlPar and const int2 count   (ref :2635-2663)
+ *   counters     int cnt; int <Ent>Idx = cnt + count.s1;  (ref :2739-2748)
+ *   locals       <nam>, <nam>[MaxDeg][NmbItm], <nam>Deg, <nam>Nul,
+ *                #define <nam>DegMax, voyeurs <Voy>[]      (ref :2670-2732)
+ *   reads        downlinks, neighbour links, balls with voyeurs (ref :2755-2885)
+ *   body         verbatim after dialect rewriting           (ref :2892-2896)
+ *   writes       <nam>Tab[cnt + count.s1] = <nam>            (ref :2903-2938)
+ *
+ * The GB300 difference is in the uplink (ball/shell) gathers.  The reference
+ * fills, for every ball entry k < DegMax and every item j, a per-thread array
+ * X[k][j] with a conditional global load (128 float4 loads and 2 KB of
+ * private memory per vertex for the NodeSmoothing gather).  In "lazy" mode
+ * the generator declares X as an accessor object (gml_up / gml_up1 in
+ * gml_cl.h) whose operator[] performs the load the body actually asks for,
+ * with the same value (null beyond the degree).  The ball row, the voyeur
+ * indices and the link vectors are accessors too.  Bodies that need real
+ * arrays (writing into a gathered local, taking its address) fail to compile
+ * in lazy mode and are regenerated in "eager" mode, which reproduces the
+ * reference's prologue statement by statement.
+ *
+ * Read-only arguments are passed as const __restrict__ pointers so that the
+ * compiler can route their loads through the read-only data path.
+ */
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "gml_internal.h"
+
+typedef struct { char *buf; size_t len, cap; } Out;
+
+static void emit(Out *o, const char *fmt, ...)
+{
+   va_list ap;
+   int n;
+   for(;;)
+   {
+      size_t room = o->cap - o->len;
+      va_start(ap, fmt);
+      n = vsnprintf(o->buf + o->len, room, fmt, ap);
+      va_end(ap);
+      if(n >= 0 && (size_t)n < room)
+      {
+         o->len += n;
+         return;
+      }
+      o->cap = o->cap * 2 + (size_t)n + 1024;
+      o->buf = realloc(o->buf, o->cap);
+   }
+}
+
+static const char HexDig[] = "0123456789abcdef";
+
+static int is_read_only(const GmlArgSct *a)
+{
+   return !(a->FlgTab & GmlWriteMode) && !(a->FlgTab & GmlManual);
+}
+
+/* lazy accessor for an uplinked (count-linked) datatype? */
+static int lazy_data(const GmlArgSct *a, const GmlArgSct *cpt, int lazy)
+{
+   return lazy && cpt && (a->FlgTab & GmlReadMode) && is_read_only(a);
+}
+
+int gml_generate(char **res, const char *PrcNam, int MshTyp, int NmbArg,
+                 const GmlArgSct *ArgTab, const char *KrnSrc, const char *UsrTlk,
+                 const char *ParSrc, int lazy)
+{
+   Out o;
+   int i, j, k, l;
+   char *tmp;
+
+   o.cap = 16384;
+   o.len = 0;
+   o.buf = malloc(o.cap);
+   o.buf[0] = 0;
+
+   emit(&o, "// GMlib GB300 generated kernel: %s (%s prologue)\n", PrcNam, lazy ? "lazy" : "eager");
+   emit(&o, "#include \"gml_cl.h\"\n");
+   emit(&o, "// GMlib MESHING AND GEOMETRICAL TOOLKIT\n#include \"gml_toolkit.h\"\n");
+
+   if(UsrTlk)
+   {
+      tmp = gml_rewrite_opencl(UsrTlk);
+      emit(&o, "// USER'S TOOLKIT\n%s\n", tmp);
+      free(tmp);
+   }
+
+   emit(&o, "// USER'S ARGUMENTS STRUCTURE\n");
+   if(ParSrc)
+   {
+      tmp = gml_rewrite_opencl(ParSrc);
+      emit(&o, "%s\n", tmp);
+      free(tmp);
+   }
+   else
+      emit(&o, "typedef struct { int foo; float res; } GmlParSct;\n");
+
+   /* ---------------- header ---------------- */
+   emit(&o, "// KERNEL HEADER\nextern \"C\" __global__ void %s(", PrcNam);
+
+   for(i=0;i<NmbArg;i++)
+   {
+      const GmlArgSct *a = &ArgTab[i];
+      const char *cq = is_read_only(a) ? "const " : "";
+      const char *rq = is_read_only(a) ? "__restrict__ " : "";
+      if(a->NmbItm <= 1)
+         emit(&o, "\n   %s%s *%s%sTab,", cq, GmlOclTypStr[ a->ItmTyp ], rq, a->nam);
+      else
+         emit(&o, "\n   %s%s (*%s%sTab)[%d],", cq, GmlOclTypStr[ a->ItmTyp ], rq, a->nam, a->NmbItm);
+   }
+   emit(&o, "\n   GmlParSct *GmlPar,\n   const int2 count )\n{\n");
+
+   /* ---------------- counters ---------------- */
+   emit(&o, "// KERNEL COUNTERS\n");
+   emit(&o, "   int cnt = get_global_id(0);\n");
+   emit(&o, "   int %sIdx = cnt + count.s1;\n\n", GmlBalTypStr[ MshTyp ]);
+   emit(&o, "   if(cnt >= count.s0)\n      return;\n\n");
+
+   /* ---------------- variables ---------------- */
+   emit(&o, "// KERNEL VARIABLES DEFINITION\n");
+
+   for(i=0;i<NmbArg;i++)
+   {
+      const GmlArgSct *a = &ArgTab[i];
+      const GmlArgSct *lnk = a->LnkIdx != -1 ? &ArgTab[ a->LnkIdx ] : NULL;
+      const GmlArgSct *cpt = a->CntIdx != -1 ? &ArgTab[ a->CntIdx ] : NULL;
+      const char *T = GmlOclTypStr[ a->ItmTyp ];
+
+      if(a->FlgTab & GmlManual)
+         continue;
+
+      /* accessors are declared after the eager reads they depend on */
+      if(lazy_data(a, cpt, lazy))
+         continue;
+      if(lazy && a->LnkDir == 1 && a->NmbItm > 1 && (a->FlgTab & GmlReadMode))
+         continue;
+
+      if(lnk && lnk->MaxDeg > 1)
+      {
+         if(a->NmbItm > 1)
+            emit(&o, "   %s %s[%d][%d];\n", T, a->nam, lnk->MaxDeg, a->NmbItm);
+         else
+            emit(&o, "   %s %s[%d];\n", T, a->nam, lnk->MaxDeg);
+      }
+      else
+      {
+         if(a->NmbItm > 1)
+            emit(&o, "   %s %s[%d];\n", T, a->nam, a->NmbItm);
+         else
+            emit(&o, "   %s %s;\n", T, a->nam);
+      }
+
+      if(cpt)
+      {
+         emit(&o, "   %s %sDeg;\n", GmlOclTypStr[ cpt->ItmTyp ], a->nam);
+         emit(&o, "   %s %sNul;\n", T, a->nam);
+         emit(&o, "   #define   %sDegMax %d\n", a->nam, lnk->MaxDeg);
+      }
+      else if(lnk && lnk->LnkDir == 0)
+         emit(&o, "   %s %sNul;\n", T, a->nam);
+
+      if(a->FlgTab & GmlVoyeurs)
+         emit(&o, "   char      %s[%d];\n", a->VoyNam, a->NmbItm * a->ItmLen);
+   }
+
+   /* ---------------- reads ---------------- */
+   emit(&o, "\n// KERNEL MEMORY READINGS\n");
+
+   for(i=0;i<NmbArg;i++)
+   {
+      const GmlArgSct *a = &ArgTab[i];
+      const GmlArgSct *lnk = a->LnkIdx != -1 ? &ArgTab[ a->LnkIdx ] : NULL;
+      const GmlArgSct *cpt = a->CntIdx != -1 ? &ArgTab[ a->CntIdx ] : NULL;
+      int siz;
+
+      if(!(a->FlgTab & GmlReadMode) || (a->FlgTab & GmlManual))
+         continue;
+      if(lazy_data(a, cpt, lazy))
+         continue;
+      if(lazy && a->LnkDir == 1 && a->NmbItm > 1)
+         continue;
+
+      siz = (lnk && lnk->NmbItm * lnk->ItmLen > 1) ? lnk->NmbItm * lnk->ItmLen : 1;
+
+      for(j=0;j<a->NmbItm;j++)
+      {
+         char ArgTd1[32] = "", LnkNam[256], CptNam[256] = "";
+
+         if(cpt)
+         {
+            snprintf(CptNam, sizeof(CptNam), "%sDeg", a->nam);
+            emit(&o, "   %s = %s;\n", CptNam, cpt->nam);
+            emit(&o, "   %sNul = gml_zero<%s>();\n", a->nam, GmlOclTypStr[ a->ItmTyp ]);
+         }
+         else if(lnk && lnk->LnkDir == 0)
+            emit(&o, "   %sNul = gml_zero<%s>();\n", a->nam, GmlOclTypStr[ a->ItmTyp ]);
+
+         if(a->NmbItm > 1)
+            snprintf(ArgTd1, sizeof(ArgTd1), "[%d]", j);
+
+         if(lnk)
+            snprintf(LnkNam, sizeof(LnkNam), "%s", lnk->nam);
+         else if(a->LnkDir == 1)
+            snprintf(LnkNam, sizeof(LnkNam), "cnt");
+         else
+            snprintf(LnkNam, sizeof(LnkNam), "cnt + count.s1");
+
+         if(a->FlgTab & GmlVoyeurs)
+         {
+            emit(&o, "   %s%s = %sTab[ %s ]%s;\n", a->nam, ArgTd1, a->nam, LnkNam, ArgTd1);
+            for(l=0;l<a->ItmLen;l++)
+               emit(&o, "   %s[%d] = %s%s.s%c & 7;\n", a->VoyNam, j * a->ItmLen + l,
+                    a->nam, ArgTd1, HexDig[l]);
+            emit(&o, "   %s%s = %s%s >> 4;\n", a->nam, ArgTd1, a->nam, ArgTd1);
+            continue;
+         }
+
+         for(k=0;k<siz;k++)
+         {
+            char ArgTd2[32] = "", LnkTd1[32] = "", LnkTd2[16] = "", DegTst[300] = "", DegNul[300] = "";
+            const char *BalSft = a->LnkDir == 1 ? ">> 4" : "";
+
+            if(siz > 1)
+               snprintf(ArgTd2, sizeof(ArgTd2), "[%d]", k);
+            if(lnk && lnk->NmbItm > 1)
+               snprintf(LnkTd1, sizeof(LnkTd1), "[%d]", k / 16);
+            if(lnk && lnk->ItmLen > 1)
+               snprintf(LnkTd2, sizeof(LnkTd2), ".s%c", HexDig[ k & 15 ]);
+
+            if(cpt)
+            {
+               snprintf(DegTst, sizeof(DegTst), "(%s >= %d) ?", CptNam, k + 1);
+               snprintf(DegNul, sizeof(DegNul), ": %sNul", a->nam);
+            }
+            else if(lnk && lnk->LnkDir == 0)
+            {
+               snprintf(DegTst, sizeof(DegTst), "%s%s ?", lnk->nam, LnkTd2);
+               snprintf(DegNul, sizeof(DegNul), ": %sNul", a->nam);
+            }
+
+            emit(&o, "   %s%s%s = %s %sTab[ %s%s%s ]%s %s %s;\n",
+                 a->nam, ArgTd2, ArgTd1, DegTst, a->nam, LnkNam, LnkTd1, LnkTd2, ArgTd1,
+                 BalSft, DegNul);
+         }
+      }
+      emit(&o, "\n");
+   }
+
+   /* ---------------- lazy accessors ---------------- */
+   if(lazy)
+      for(i=0;i<NmbArg;i++)
+      {
+         const GmlArgSct *a = &ArgTab[i];
+         const GmlArgSct *lnk = a->LnkIdx != -1 ? &ArgTab[ a->LnkIdx ] : NULL;
+         const GmlArgSct *cpt = a->CntIdx != -1 ? &ArgTab[ a->CntIdx ] : NULL;
+         const char *T = GmlOclTypStr[ a->ItmTyp ];
+
+         if(a->FlgTab & GmlManual)
+            continue;
+
+         if(lazy_data(a, cpt, lazy))
+         {
+            /* uplinked datatype: degree, null value, bound and accessor */
+            emit(&o, "   %s %sDeg = %s;\n", GmlOclTypStr[ cpt->ItmTyp ], a->nam, cpt->nam);
+            emit(&o, "   %s %sNul = gml_zero<%s>();\n", T, a->nam, T);
+            emit(&o, "   #define   %sDegMax %d\n", a->nam, lnk->MaxDeg);
+            if(a->NmbItm > 1)
+               emit(&o, "   const gml_up<%s,%d> %s = { %sTab, (const int *)(%sTab + cnt), %sDeg };\n",
+                    T, a->NmbItm, a->nam, a->nam, lnk->nam, a->nam);
+            else
+               emit(&o, "   const gml_up1<%s> %s = { %sTab, (const int *)(%sTab + cnt), %sDeg };\n",
+                    T, a->nam, a->nam, lnk->nam, a->nam);
+         }
+         else if(a->LnkDir == 1 && a->NmbItm > 1 && (a->FlgTab & GmlReadMode))
+         {
+            /* ball row as link vectors shifted on access */
+            emit(&o, "   const gml_ballink<%s> %s = { (const %s *)(%sTab + cnt) };\n", T, a->nam, T, a->nam);
+            if(a->FlgTab & GmlVoyeurs)
+               emit(&o, "   const gml_voy %s = { (const int *)(%sTab + cnt) };\n", a->VoyNam, a->nam);
+         }
+      }
+
+   /* ---------------- user body ---------------- */
+   tmp = gml_rewrite_opencl(KrnSrc);
+   emit(&o, "// USER'S KERNEL CODE\n%s\n", tmp);
+   free(tmp);
+
+   /* ---------------- writes ---------------- */
+   emit(&o, "\n// KERNEL MEMORY WRITINGS\n");
+
+   for(i=0;i<NmbArg;i++)
+   {
+      const GmlArgSct *a = &ArgTab[i];
+
+      if(!(a->FlgTab & GmlWriteMode) || (a->FlgTab & GmlManual))
+         continue;
+
+      if(a->NmbItm == 1)
+         emit(&o, "   %sTab[ cnt + count.s1 ] = %s;\n", a->nam, a->nam);
+      else
+         for(j=0;j<a->NmbItm;j++)
+            emit(&o, "   %sTab[ cnt + count.s1 ][%d] = %s[%d];\n", a->nam, j, a->nam, j);
+   }
+
+   emit(&o, "}\n");
+
+   *res = o.buf;
+   return 1;
+}

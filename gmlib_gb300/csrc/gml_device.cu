@@ -1,0 +1,416 @@
+/*
+ * gml_device.cu -- CUDA side of the thin C ABI declared in gml_device.h.
+ *
+ * One GmlInit instance owns one non-blocking CUDA stream on the selected
+ * device; every copy and launch of the instance is ordered on that stream
+ * (the reference uses one in-order OpenCL queue per instance,
+ * sources/gmlib3.c:437-438).  Generated kernels are compiled by NVRTC straight
+ * to an sm_103a cubin and loaded through the driver API, whose entry points
+ * are fetched from the runtime (cudaGetDriverEntryPoint) so that the library
+ * loads on hosts without a GPU driver.
+ */
+#include <cuda_runtime.h>
+#include <cuda.h>
+#include <nvrtc.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "gml_device.h"
+
+/* embedded headers for NVRTC (generated at build time from gml_cl.h and
+   gml_toolkit.h) */
+extern "C" const char *gml_embedded_cl_h;
+extern "C" const char *gml_embedded_toolkit_h;
+
+struct GmdCtx
+{
+   int            dev, nsm;
+   cudaStream_t   stream;
+   char           err[512];
+};
+
+/* ------------------------------------------------------------------------- */
+/* driver API entry points                                                    */
+/* ------------------------------------------------------------------------- */
+
+typedef CUresult (*PFN_ModuleLoadData)(CUmodule *, const void *);
+typedef CUresult (*PFN_ModuleGetFunction)(CUfunction *, CUmodule, const char *);
+typedef CUresult (*PFN_ModuleUnload)(CUmodule);
+typedef CUresult (*PFN_LaunchKernel)(CUfunction, unsigned, unsigned, unsigned,
+                                     unsigned, unsigned, unsigned, unsigned,
+                                     CUstream, void **, void **);
+typedef CUresult (*PFN_FuncGetAttribute)(int *, CUfunction_attribute, CUfunction);
+typedef CUresult (*PFN_FuncSetAttribute)(CUfunction, CUfunction_attribute, int);
+
+static PFN_ModuleLoadData     p_cuModuleLoadData;
+static PFN_ModuleGetFunction  p_cuModuleGetFunction;
+static PFN_ModuleUnload       p_cuModuleUnload;
+static PFN_LaunchKernel       p_cuLaunchKernel;
+static PFN_FuncGetAttribute   p_cuFuncGetAttribute;
+static PFN_FuncSetAttribute   p_cuFuncSetAttribute;
+
+static int load_driver_api(char *err, int errlen)
+{
+   cudaDriverEntryPointQueryResult q;
+   if(p_cuLaunchKernel)
+      return 1;
+#define GET(sym, ptr) \
+   if(cudaGetDriverEntryPointByVersion(sym, (void **)&ptr, 12000, cudaEnableDefault, &q) != cudaSuccess \
+      || q != cudaDriverEntryPointSuccess || !ptr) \
+   { snprintf(err, errlen, "driver entry point %s unavailable", sym); return 0; }
+   GET("cuModuleLoadData", p_cuModuleLoadData);
+   GET("cuModuleGetFunction", p_cuModuleGetFunction);
+   GET("cuModuleUnload", p_cuModuleUnload);
+   GET("cuFuncGetAttribute", p_cuFuncGetAttribute);
+   GET("cuFuncSetAttribute", p_cuFuncSetAttribute);
+   GET("cuLaunchKernel", p_cuLaunchKernel);
+#undef GET
+   return 1;
+}
+
+static int ok(GmdCtx *ctx, cudaError_t e, const char *what)
+{
+   if(e == cudaSuccess)
+      return 1;
+   if(ctx)
+      snprintf(ctx->err, sizeof(ctx->err), "%s: %s", what, cudaGetErrorString(e));
+   fprintf(stderr, "GMlib CUDA error in %s: %s\n", what, cudaGetErrorString(e));
+   return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* device and context                                                         */
+/* ------------------------------------------------------------------------- */
+
+extern "C" int gmd_device_count(void)
+{
+   int n = 0;
+   if(cudaGetDeviceCount(&n) != cudaSuccess)
+   {
+      cudaGetLastError();
+      return 0;
+   }
+   return n;
+}
+
+extern "C" int gmd_device_name(int dev, char *buf, int len)
+{
+   cudaDeviceProp p;
+   if(cudaGetDeviceProperties(&p, dev) != cudaSuccess)
+      return 0;
+   snprintf(buf, len, "%s", p.name);
+   return 1;
+}
+
+extern "C" GmdCtx *gmd_init(int dev, int *fp64, char *err, int errlen)
+{
+   GmdCtx *ctx;
+   int n = gmd_device_count();
+   cudaDeviceProp p;
+
+   if(dev < 0 || dev >= n)
+   {
+      snprintf(err, errlen, "Selected device Id is out of bounds (0 -> %d)", n - 1);
+      return NULL;
+   }
+   if(cudaSetDevice(dev) != cudaSuccess || cudaFree(0) != cudaSuccess)
+   {
+      snprintf(err, errlen, "cannot initialise device %d", dev);
+      return NULL;
+   }
+   if(!load_driver_api(err, errlen))
+      return NULL;
+
+   ctx = (GmdCtx *)calloc(1, sizeof(GmdCtx));
+   if(!ctx)
+      return NULL;
+   ctx->dev = dev;
+   cudaGetDeviceProperties(&p, dev);
+   ctx->nsm = p.multiProcessorCount;
+
+   if(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+   {
+      snprintf(err, errlen, "cannot create a CUDA stream");
+      free(ctx);
+      return NULL;
+   }
+   if(fp64)
+      *fp64 = 1;   /* every sm_103a device has FP64 units */
+   return ctx;
+}
+
+extern "C" void gmd_stop(GmdCtx *ctx)
+{
+   if(!ctx)
+      return;
+   cudaSetDevice(ctx->dev);
+   cudaStreamSynchronize(ctx->stream);
+   cudaStreamDestroy(ctx->stream);
+   free(ctx);
+}
+
+extern "C" int gmd_sync(GmdCtx *ctx)
+{
+   if(!ctx)
+      return 1;
+   return ok(ctx, cudaStreamSynchronize(ctx->stream), "stream synchronize");
+}
+
+extern "C" void *gmd_stream(GmdCtx *ctx) { return ctx ? (void *)ctx->stream : NULL; }
+extern "C" const char *gmd_last_error(GmdCtx *ctx) { return ctx ? ctx->err : ""; }
+extern "C" int gmd_num_sms(GmdCtx *ctx) { return ctx ? ctx->nsm : 1; }
+
+extern "C" size_t gmd_free_memory(GmdCtx *ctx)
+{
+   size_t f = 0, t = 0;
+   (void)ctx;
+   cudaMemGetInfo(&f, &t);
+   return f;
+}
+
+/* ------------------------------------------------------------------------- */
+/* memory                                                                     */
+/* ------------------------------------------------------------------------- */
+
+extern "C" void *gmd_alloc(GmdCtx *ctx, size_t bytes)
+{
+   void *p = NULL;
+   if(!bytes)
+      bytes = 16;
+   if(!ctx)                       /* offline instance: host memory */
+      return calloc(1, bytes);
+   if(!ok(ctx, cudaMallocAsync(&p, bytes, ctx->stream), "device allocation"))
+      return NULL;
+   if(!ok(ctx, cudaMemsetAsync(p, 0, bytes, ctx->stream), "device clear"))
+      return NULL;
+   return p;
+}
+
+extern "C" void gmd_free(GmdCtx *ctx, void *ptr)
+{
+   if(ptr && !ctx)
+      free(ptr);
+   else if(ptr)
+      cudaFreeAsync(ptr, ctx->stream);
+}
+
+extern "C" void *gmd_host_alloc(size_t bytes)
+{
+   void *p = NULL;
+   if(!bytes)
+      bytes = 16;
+   if(cudaMallocHost(&p, bytes) != cudaSuccess)
+   {
+      cudaGetLastError();
+      return NULL;
+   }
+   memset(p, 0, bytes);
+   return p;
+}
+
+extern "C" void gmd_host_free(void *ptr)
+{
+   if(ptr)
+      cudaFreeHost(ptr);
+}
+
+extern "C" int gmd_h2d_async(GmdCtx *ctx, void *dst, const void *src, size_t bytes)
+{
+   if(!ctx) { memcpy(dst, src, bytes); return 1; }
+   return ok(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream), "upload");
+}
+
+extern "C" int gmd_d2h(GmdCtx *ctx, void *dst, const void *src, size_t bytes)
+{
+   if(!ctx) { memcpy(dst, src, bytes); return 1; }
+   if(!ok(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download"))
+      return 0;
+   return ok(ctx, cudaStreamSynchronize(ctx->stream), "download synchronize");
+}
+
+extern "C" int gmd_d2d_async(GmdCtx *ctx, void *dst, const void *src, size_t bytes)
+{
+   if(!ctx) { memmove(dst, src, bytes); return 1; }
+   return ok(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, ctx->stream), "device copy");
+}
+
+extern "C" int gmd_memset_async(GmdCtx *ctx, void *dst, int val, size_t bytes)
+{
+   if(!ctx) { memset(dst, val, bytes); return 1; }
+   return ok(ctx, cudaMemsetAsync(dst, val, bytes, ctx->stream), "device memset");
+}
+
+/* ------------------------------------------------------------------------- */
+/* events                                                                     */
+/* ------------------------------------------------------------------------- */
+
+extern "C" void *gmd_event_new(void)
+{
+   cudaEvent_t e;
+   if(cudaEventCreate(&e) != cudaSuccess)
+      return NULL;
+   return (void *)e;
+}
+
+extern "C" void gmd_event_free(void *evt)
+{
+   if(evt)
+      cudaEventDestroy((cudaEvent_t)evt);
+}
+
+extern "C" int gmd_event_record(GmdCtx *ctx, void *evt)
+{
+   if(!ctx || !evt)
+      return 0;
+   return ok(ctx, cudaEventRecord((cudaEvent_t)evt, ctx->stream), "event record");
+}
+
+extern "C" int gmd_event_wait(void *evt)
+{
+   if(!evt)
+      return 1;
+   return cudaEventSynchronize((cudaEvent_t)evt) == cudaSuccess;
+}
+
+extern "C" double gmd_event_elapsed_s(void *beg, void *end)
+{
+   float ms = 0.f;
+   if(!beg || !end)
+      return 0.;
+   if(cudaEventSynchronize((cudaEvent_t)end) != cudaSuccess)
+      return 0.;
+   if(cudaEventElapsedTime(&ms, (cudaEvent_t)beg, (cudaEvent_t)end) != cudaSuccess)
+   {
+      cudaGetLastError();
+      return 0.;
+   }
+   return 1e-3 * (double)ms;
+}
+
+extern "C" int gmd_capturing(GmdCtx *ctx)
+{
+   cudaStreamCaptureStatus s = cudaStreamCaptureStatusNone;
+   if(!ctx)
+      return 0;
+   cudaStreamIsCapturing(ctx->stream, &s);
+   return s != cudaStreamCaptureStatusNone;
+}
+
+/* ------------------------------------------------------------------------- */
+/* NVRTC                                                                      */
+/* ------------------------------------------------------------------------- */
+
+extern "C" int gmd_compile(const char *src, const char *name, const char *opts,
+                           void **cubin, size_t *cubin_size, char **log)
+{
+   nvrtcProgram prog;
+   const char *hdr[2]  = { gml_embedded_cl_h, gml_embedded_toolkit_h };
+   const char *hnam[2] = { "gml_cl.h", "gml_toolkit.h" };
+   const char *argv[64];
+   char *optbuf = NULL, *tok, *save = NULL;
+   int argc = 0, okres;
+   size_t n;
+   nvrtcResult r;
+
+   *cubin = NULL;
+   *cubin_size = 0;
+   if(log)
+      *log = NULL;
+
+   argv[argc++] = "--gpu-architecture=sm_103a";
+   argv[argc++] = "-std=c++17";
+   argv[argc++] = "--fmad=true";
+   argv[argc++] = "-default-device";
+   argv[argc++] = "-lineinfo";
+
+   if(opts && *opts)
+   {
+      optbuf = strdup(opts);
+      for(tok = strtok_r(optbuf, " \t\n", &save); tok && argc < 60;
+          tok = strtok_r(NULL, " \t\n", &save))
+         argv[argc++] = tok;
+   }
+
+   if(nvrtcCreateProgram(&prog, src, name, 2, hdr, hnam) != NVRTC_SUCCESS)
+   {
+      free(optbuf);
+      return 0;
+   }
+
+   r = nvrtcCompileProgram(prog, argc, argv);
+   okres = (r == NVRTC_SUCCESS);
+
+   if(log && nvrtcGetProgramLogSize(prog, &n) == NVRTC_SUCCESS && n > 1)
+   {
+      *log = (char *)malloc(n + 1);
+      nvrtcGetProgramLog(prog, *log);
+   }
+
+   if(okres && nvrtcGetCUBINSize(prog, &n) == NVRTC_SUCCESS && n)
+   {
+      *cubin = malloc(n);
+      nvrtcGetCUBIN(prog, (char *)*cubin);
+      *cubin_size = n;
+   }
+   else
+      okres = 0;
+
+   nvrtcDestroyProgram(&prog);
+   free(optbuf);
+   return okres;
+}
+
+extern "C" int gmd_module_load(GmdCtx *ctx, const void *cubin, const char *name,
+                               void **module, void **func, int *max_threads, int *num_regs)
+{
+   CUmodule m;
+   CUfunction f;
+   CUresult r;
+
+   if(!ctx)
+      return 0;
+   cudaSetDevice(ctx->dev);
+   if((r = p_cuModuleLoadData(&m, cubin)) != CUDA_SUCCESS)
+   {
+      snprintf(ctx->err, sizeof(ctx->err), "cuModuleLoadData failed (%d)", (int)r);
+      return 0;
+   }
+   if((r = p_cuModuleGetFunction(&f, m, name)) != CUDA_SUCCESS)
+   {
+      snprintf(ctx->err, sizeof(ctx->err), "kernel %s not found (%d)", name, (int)r);
+      p_cuModuleUnload(m);
+      return 0;
+   }
+   if(max_threads)
+      p_cuFuncGetAttribute(max_threads, CU_FUNC_ATTRIBUTE_MAX_THREADS_PER_BLOCK, f);
+   if(num_regs)
+      p_cuFuncGetAttribute(num_regs, CU_FUNC_ATTRIBUTE_NUM_REGS, f);
+   *module = (void *)m;
+   *func = (void *)f;
+   return 1;
+}
+
+extern "C" void gmd_module_unload(void *module)
+{
+   if(module && p_cuModuleUnload)
+      p_cuModuleUnload((CUmodule)module);
+}
+
+extern "C" int gmd_launch(GmdCtx *ctx, void *func, unsigned grid, unsigned block,
+                          unsigned smem, void **args)
+{
+   CUresult r;
+   if(!grid)
+      return 1;
+   if(!ctx)
+      return 0;
+   r = p_cuLaunchKernel((CUfunction)func, grid, 1, 1, block, 1, 1, smem,
+                        (CUstream)ctx->stream, args, NULL);
+   if(r != CUDA_SUCCESS)
+   {
+      snprintf(ctx->err, sizeof(ctx->err), "cuLaunchKernel failed (%d)", (int)r);
+      fprintf(stderr, "GMlib: %s\n", ctx->err);
+      return 0;
+   }
+   return 1;
+}

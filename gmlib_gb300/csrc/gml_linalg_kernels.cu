@@ -1,0 +1,275 @@
+/*
+ * gml_linalg_kernels.cu -- block sparse mat-vec and block-vector kernels.
+ *
+ * Replaces sources/multmatvec.cl (MulMatVecSlc16..256, block sizes 4 and 5;
+ * block size 7 has no kernel there), multdiagmatvec.cl, addvec.cl,
+ * scalevec.cl and normvec.cl.  All are HBM-bound streaming kernels:
+ *
+ *   SpMV     one thread per block row over the SELL-32 layout of
+ *            gml_linalg.c: column indices and block values of entry k are
+ *            128-byte runs per warp, x lines are gathered with 16-byte
+ *            vector loads (x fits in L2), y is written once.
+ *            Bytes per row: 4 (degree) + deg * (4 + 4*b*b or 8*b*b) + the
+ *            output line; the x gathers are served by L2.
+ *   vectors  grid-stride loops over 16-byte chunks.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "gml_device.h"
+#include "gml_linalg.h"
+
+#define LA_THREADS 256
+
+/* load one vector line of XS scalars with 16-byte loads */
+template<class T, int XS> __device__ __forceinline__ void load_line(const T *__restrict__ p, T *out)
+{
+   constexpr int NCH = (XS * (int)sizeof(T) + 15) / 16;
+   if((XS * sizeof(T)) % 16 == 0)
+   {
+#pragma unroll
+      for(int c=0;c<NCH;c++)
+      {
+         float4 v = __ldg(reinterpret_cast<const float4 *>(p) + c);
+         const T *t = reinterpret_cast<const T *>(&v);
+#pragma unroll
+         for(int i=0;i<(int)(16/sizeof(T));i++)
+            out[ c * (16 / sizeof(T)) + i ] = t[i];
+      }
+   }
+   else
+   {
+#pragma unroll
+      for(int i=0;i<XS;i++)
+         out[i] = __ldg(p + i);
+   }
+}
+
+template<int B, class T, int XS>
+__global__ void __launch_bounds__(LA_THREADS)
+sell_spmv_kernel(int n, const int64_t *__restrict__ soff, const int *__restrict__ deg,
+                 const int *__restrict__ col, const T *__restrict__ val,
+                 const T *__restrict__ x, T *__restrict__ y, int ys)
+{
+   int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if(r >= n)
+      return;
+
+   const int lane = r & 31;
+   const int64_t base = __ldg(&soff[ r >> 5 ]);
+   const int d = __ldg(&deg[r]);
+   const int *cp = col + base * 32 + lane;
+   const T *vp = val + base * (B * B * 32) + lane;
+   T acc[B];
+
+#pragma unroll
+   for(int i=0;i<B;i++)
+      acc[i] = (T)0;
+
+#pragma unroll 2
+   for(int k=0;k<d;k++)
+   {
+      const int c = __ldg(cp + (size_t)k * 32);
+      T xv[XS];
+      load_line<T, XS>(x + (size_t)c * XS, xv);
+      const T *blk = vp + (size_t)k * (B * B * 32);
+#pragma unroll
+      for(int i=0;i<B;i++)
+#pragma unroll
+         for(int j=0;j<B;j++)
+            acc[i] += __ldg(blk + (i * B + j) * 32) * xv[j];
+   }
+
+   T *yl = y + (size_t)r * ys;
+#pragma unroll
+   for(int i=0;i<B;i++)
+      yl[i] = acc[i];
+   for(int i=B;i<ys;i++)
+      yl[i] = (T)0;
+}
+
+template<int B, class T>
+static int launch_spmv(const GmlSellDev *A, const void *x, int xs, void *y, int ys, cudaStream_t st)
+{
+   int nb = (A->NmbLin + LA_THREADS - 1) / LA_THREADS;
+   if(xs == 4)
+      sell_spmv_kernel<B, T, 4><<<nb, LA_THREADS, 0, st>>>(A->NmbLin, A->SlcOff, A->Deg, A->Col,
+         (const T *)A->Val, (const T *)x, (T *)y, ys);
+   else if(xs == 8)
+      sell_spmv_kernel<B, T, 8><<<nb, LA_THREADS, 0, st>>>(A->NmbLin, A->SlcOff, A->Deg, A->Col,
+         (const T *)A->Val, (const T *)x, (T *)y, ys);
+   else
+      return 0;
+   return cudaGetLastError() == cudaSuccess;
+}
+
+extern "C" int gmd_sell_spmv(GmdCtx *ctx, const GmlSellDev *A, const void *x, int xs,
+                             void *y, int ys, double alpha, double beta, double *dotout, int flags)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   (void)alpha; (void)beta; (void)dotout; (void)flags;
+   if(!ctx)
+      return 0;
+   if(A->FltSiz == 4)
+   {
+      switch(A->BlkSiz)
+      {
+         case 3: return launch_spmv<3, float>(A, x, xs, y, ys, st);
+         case 4: return launch_spmv<4, float>(A, x, xs, y, ys, st);
+         case 5: return launch_spmv<5, float>(A, x, xs, y, ys, st);
+         case 7: return launch_spmv<7, float>(A, x, xs, y, ys, st);
+      }
+   }
+   else
+   {
+      switch(A->BlkSiz)
+      {
+         case 3: return launch_spmv<3, double>(A, x, xs, y, ys, st);
+         case 4: return launch_spmv<4, double>(A, x, xs, y, ys, st);
+         case 5: return launch_spmv<5, double>(A, x, xs, y, ys, st);
+         case 7: return launch_spmv<7, double>(A, x, xs, y, ys, st);
+      }
+   }
+   return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* vectors                                                                    */
+/* ------------------------------------------------------------------------- */
+
+template<class T>
+__global__ void __launch_bounds__(LA_THREADS)
+add3_kernel(const T *__restrict__ u, const T *__restrict__ v, const T *__restrict__ w,
+            T *__restrict__ y, size_t n)
+{
+   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (size_t)gridDim.x * blockDim.x;
+   for(;i<n;i+=nth)
+      y[i] = __ldg(&u[i]) + __ldg(&v[i]) + __ldg(&w[i]);
+}
+
+__global__ void __launch_bounds__(LA_THREADS)
+add3_f4_kernel(const float4 *__restrict__ u, const float4 *__restrict__ v,
+               const float4 *__restrict__ w, float4 *__restrict__ y, size_t n4)
+{
+   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (size_t)gridDim.x * blockDim.x;
+   for(;i<n4;i+=nth)
+   {
+      float4 a = __ldg(&u[i]), b = __ldg(&v[i]), c = __ldg(&w[i]);
+      y[i] = make_float4(a.x + b.x + c.x, a.y + b.y + c.y, a.z + b.z + c.z, a.w + b.w + c.w);
+   }
+}
+
+static unsigned grid_for(GmdCtx *ctx, size_t n)
+{
+   size_t g = (n + LA_THREADS - 1) / LA_THREADS, cap = (size_t)gmd_num_sms(ctx) * 8;
+   if(g > cap) g = cap;
+   return (unsigned)(g ? g : 1);
+}
+
+extern "C" int gmd_vec_add3(GmdCtx *ctx, const void *u, const void *v, const void *w, void *y,
+                            size_t n, int fltsiz)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   if(!ctx)
+      return 0;
+   if(fltsiz == 4 && n % 4 == 0)
+      add3_f4_kernel<<<grid_for(ctx, n / 4), LA_THREADS, 0, st>>>((const float4 *)u, (const float4 *)v,
+         (const float4 *)w, (float4 *)y, n / 4);
+   else if(fltsiz == 4)
+      add3_kernel<float><<<grid_for(ctx, n), LA_THREADS, 0, st>>>((const float *)u, (const float *)v,
+         (const float *)w, (float *)y, n);
+   else
+      add3_kernel<double><<<grid_for(ctx, n), LA_THREADS, 0, st>>>((const double *)u, (const double *)v,
+         (const double *)w, (double *)y, n);
+   return cudaGetLastError() == cudaSuccess;
+}
+
+template<class T>
+__global__ void __launch_bounds__(LA_THREADS) scale_kernel(T *__restrict__ u, size_t n, T s)
+{
+   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (size_t)gridDim.x * blockDim.x;
+   for(;i<n;i+=nth)
+      u[i] *= s;
+}
+
+extern "C" int gmd_vec_scale(GmdCtx *ctx, void *u, size_t n, int fltsiz, double s)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   if(!ctx)
+      return 0;
+   if(fltsiz == 4)
+      scale_kernel<float><<<grid_for(ctx, n), LA_THREADS, 0, st>>>((float *)u, n, (float)s);
+   else
+      scale_kernel<double><<<grid_for(ctx, n), LA_THREADS, 0, st>>>((double *)u, n, s);
+   return cudaGetLastError() == cudaSuccess;
+}
+
+template<class T>
+__global__ void __launch_bounds__(LA_THREADS)
+rownorm_kernel(const T *__restrict__ u, int us, int nl, int nlin, float *__restrict__ out)
+{
+   int l = blockIdx.x * blockDim.x + threadIdx.x;
+   if(l >= nlin)
+      return;
+   T s = (T)0;
+   for(int c=0;c<nl;c++)
+   {
+      T x = __ldg(&u[ (size_t)l * us + c ]);
+      s += x * x;
+   }
+   out[l] = (float)sqrt(s);
+}
+
+extern "C" int gmd_vec_rownorm(GmdCtx *ctx, const void *u, int us, int nlanes, int fltsiz,
+                               int nlin, float *out)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   int nb = (nlin + LA_THREADS - 1) / LA_THREADS;
+   if(!ctx)
+      return 0;
+   if(fltsiz == 4)
+      rownorm_kernel<float><<<nb, LA_THREADS, 0, st>>>((const float *)u, us, nlanes, nlin, out);
+   else
+      rownorm_kernel<double><<<nb, LA_THREADS, 0, st>>>((const double *)u, us, nlanes, nlin, out);
+   return cudaGetLastError() == cudaSuccess;
+}
+
+template<class T>
+__global__ void __launch_bounds__(LA_THREADS)
+diag_kernel(const T *__restrict__ d, int ds, const T *__restrict__ u, T *__restrict__ v,
+            int vs, int b, int nlin)
+{
+   int l = blockIdx.x * blockDim.x + threadIdx.x;
+   if(l >= nlin)
+      return;
+   const T *dl = d + (size_t)l * ds;
+   const T *ul = u + (size_t)l * vs;
+   T *vl = v + (size_t)l * vs;
+   T x[8];
+   for(int j=0;j<b && j<8;j++)
+      x[j] = __ldg(&ul[j]);
+   for(int i=0;i<b;i++)
+   {
+      T s = (T)0;
+      for(int j=0;j<b && j<8;j++)
+         s += __ldg(&dl[ i * b + j ]) * x[j];
+      vl[i] = s;
+   }
+   for(int i=b;i<vs;i++)
+      vl[i] = (T)0;
+}
+
+extern "C" int gmd_vec_diag(GmdCtx *ctx, const void *d, int ds, const void *u, void *v, int vs,
+                            int b, int fltsiz, int nlin)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   int nb = (nlin + LA_THREADS - 1) / LA_THREADS;
+   if(!ctx || b > 8)
+      return 0;
+   if(fltsiz == 4)
+      diag_kernel<float><<<nb, LA_THREADS, 0, st>>>((const float *)d, ds, (const float *)u,
+                                                    (float *)v, vs, b, nlin);
+   else
+      diag_kernel<double><<<nb, LA_THREADS, 0, st>>>((const double *)d, ds, (const double *)u,
+                                                     (double *)v, vs, b, nlin);
+   return cudaGetLastError() == cudaSuccess;
+}

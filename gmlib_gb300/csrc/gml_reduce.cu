@@ -1,0 +1,314 @@
+/*
+ * gml_reduce.cu -- single-pass reductions of a float field.
+ *
+ * Replaces the reference's reduce.cl kernels (sources/reduce.cl:6-137) and the
+ * serial CPU finish of GmlReduceVector (sources/gmlib3.c:3297-3327).  The
+ * reference reduces each work-group in __local memory, downloads one partial
+ * per group and finishes on the host in float, dropping the last partial
+ * group when the line count is not a multiple of the group size (:3299).
+ * Here one launch does everything:
+ *
+ *   - each thread streams float4 chunks (grid-stride, 16-byte loads) and
+ *     accumulates sums with an error-free TwoSum pair in FP32, so the FP64
+ *     units (a small fraction of FP32 throughput on this part) are not on the
+ *     per-element path;
+ *   - the warp folds with __shfl_xor_sync, the block through shared memory,
+ *     and the block result is stored in FP64;
+ *   - the last block to finish (ticket counter) folds the block results in
+ *     FP64 and writes the final value, then re-arms the counter.
+ *
+ * Operations (enum reduction_opp of gmlib3.h): Min, Max, Sum, L0 (number of
+ * non-zero values), L1 (sum of |x|), L2 (sum of x^2, no square root, as the
+ * reference), Linf (max |x|).
+ *
+ * Scratch layout (device, bytes): [0,8) ticket counter, [8,16) result,
+ * [16, 16 + 16*nblk) per-block partials (two doubles each).
+ */
+#include <cuda_runtime.h>
+#include <float.h>
+#include <stdint.h>
+#include <string.h>
+#include "gml_device.h"
+
+#define RED_THREADS 512
+#define RED_MAXBLK  1024
+
+struct GmdCtx;   /* opaque here; stream obtained through gmd_stream */
+
+__device__ __forceinline__ void two_sum(float &s, float &c, float x)
+{
+   float t = s + x;
+   float bp = t - s;
+   c += (s - (t - bp)) + (x - bp);
+   s = t;
+}
+
+template<int OP> __device__ __forceinline__ void red_elem(float x, float &s, float &c)
+{
+   if(OP == 0)      s = fminf(s, x);
+   else if(OP == 1) s = fmaxf(s, x);
+   else if(OP == 2) two_sum(s, c, x);
+   else if(OP == 3) s += (x != 0.0f) ? 1.0f : 0.0f;      /* counts stay exact below 2^24 per thread */
+   else if(OP == 4) two_sum(s, c, fabsf(x));
+   else if(OP == 5) two_sum(s, c, x * x);
+   else             s = fmaxf(s, fabsf(x));
+}
+
+template<int OP> __device__ __forceinline__ double red_join(double a, double b)
+{
+   if(OP == 0) return fmin(a, b);
+   if(OP == 1 || OP == 6) return fmax(a, b);
+   return a + b;
+}
+
+template<int OP> __device__ __forceinline__ float red_init()
+{
+   if(OP == 0) return FLT_MAX;
+   if(OP == 1) return -FLT_MAX;
+   return 0.0f;
+}
+
+template<int OP>
+__global__ void __launch_bounds__(RED_THREADS)
+gml_reduce_f32_kernel(const float *__restrict__ in, int n, unsigned long long *scratch)
+{
+   unsigned long long *ticket = scratch;
+   double *result  = (double *)(scratch + 1);
+   double *partial = (double *)(scratch + 2);
+   __shared__ double sh[ RED_THREADS / 32 ];
+   __shared__ int last;
+
+   float s = red_init<OP>(), c = 0.0f;
+   int tid = blockIdx.x * blockDim.x + threadIdx.x;
+   int nth = gridDim.x * blockDim.x;
+   int n4 = ((((uintptr_t)in) & 15) == 0) ? n >> 2 : 0;
+   const float4 *in4 = (const float4 *)in;
+
+   for(int i=tid;i<n4;i+=nth)
+   {
+      float4 v = __ldg(&in4[i]);
+      red_elem<OP>(v.x, s, c); red_elem<OP>(v.y, s, c);
+      red_elem<OP>(v.z, s, c); red_elem<OP>(v.w, s, c);
+   }
+   for(int i=4*n4+tid;i<n;i+=nth)
+      red_elem<OP>(__ldg(&in[i]), s, c);
+
+   double d = (double)s + (double)c;
+   for(int o=16;o>0;o>>=1)
+      d = red_join<OP>(d, __shfl_xor_sync(0xffffffffu, d, o));
+   if((threadIdx.x & 31) == 0)
+      sh[ threadIdx.x >> 5 ] = d;
+   __syncthreads();
+   if(threadIdx.x < 32)
+   {
+      d = threadIdx.x < (blockDim.x >> 5) ? sh[ threadIdx.x ] : (double)red_init<OP>();
+      for(int o=16;o>0;o>>=1)
+         d = red_join<OP>(d, __shfl_xor_sync(0xffffffffu, d, o));
+      if(threadIdx.x == 0)
+      {
+         partial[ blockIdx.x ] = d;
+         __threadfence();
+         last = (atomicAdd(ticket, 1ULL) == (unsigned long long)(gridDim.x - 1));
+      }
+   }
+   __syncthreads();
+   if(!last)
+      return;
+
+   /* last block: fold the per-block partials in FP64 */
+   __threadfence();
+   d = (double)red_init<OP>();
+   for(int i=threadIdx.x;i<(int)gridDim.x;i+=blockDim.x)
+      d = red_join<OP>(d, ((volatile double *)partial)[i]);
+   for(int o=16;o>0;o>>=1)
+      d = red_join<OP>(d, __shfl_xor_sync(0xffffffffu, d, o));
+   if((threadIdx.x & 31) == 0)
+      sh[ threadIdx.x >> 5 ] = d;
+   __syncthreads();
+   if(threadIdx.x == 0)
+   {
+      for(int w=1;w<(int)(blockDim.x >> 5);w++)
+         d = red_join<OP>(d, sh[w]);
+      *result = d;
+      *ticket = 0ULL;
+   }
+}
+
+/* ------------------------------------------------------------------------- */
+/* min / argmin / max / argmax with smallest-index ties                       */
+/* ------------------------------------------------------------------------- */
+
+/* order-preserving map of a float to an unsigned key */
+__device__ __forceinline__ unsigned fkey(float f)
+{
+   unsigned u = __float_as_uint(f);
+   return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ float funkey(unsigned k)
+{
+   return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+__global__ void __launch_bounds__(RED_THREADS)
+gml_minmax_arg_kernel(const float *__restrict__ in, int n, unsigned long long *scratch)
+{
+   /* scratch: [0] ticket, [1] min key, [2] max key (inverted), [3..] partials */
+   unsigned long long *ticket = scratch;
+   unsigned long long *part = scratch + 3;
+   __shared__ unsigned long long shmin[ RED_THREADS / 32 ], shmax[ RED_THREADS / 32 ];
+   __shared__ int last;
+   unsigned long long kmin = ~0ULL, kmax = ~0ULL;
+   int tid = blockIdx.x * blockDim.x + threadIdx.x;
+   int nth = gridDim.x * blockDim.x;
+
+   for(int i=tid;i<n;i+=nth)
+   {
+      unsigned k = fkey(__ldg(&in[i]));
+      unsigned long long a = ((unsigned long long)k << 32) | (unsigned)i;
+      unsigned long long b = ((unsigned long long)(~k) << 32) | (unsigned)i;
+      kmin = a < kmin ? a : kmin;
+      kmax = b < kmax ? b : kmax;
+   }
+   for(int o=16;o>0;o>>=1)
+   {
+      unsigned long long x = __shfl_xor_sync(0xffffffffu, kmin, o);
+      unsigned long long y = __shfl_xor_sync(0xffffffffu, kmax, o);
+      kmin = x < kmin ? x : kmin;
+      kmax = y < kmax ? y : kmax;
+   }
+   if((threadIdx.x & 31) == 0)
+   {
+      shmin[ threadIdx.x >> 5 ] = kmin;
+      shmax[ threadIdx.x >> 5 ] = kmax;
+   }
+   __syncthreads();
+   if(threadIdx.x == 0)
+   {
+      for(int w=1;w<(int)(blockDim.x >> 5);w++)
+      {
+         kmin = shmin[w] < kmin ? shmin[w] : kmin;
+         kmax = shmax[w] < kmax ? shmax[w] : kmax;
+      }
+      part[ 2 * blockIdx.x ] = kmin;
+      part[ 2 * blockIdx.x + 1 ] = kmax;
+      __threadfence();
+      last = (atomicAdd(ticket, 1ULL) == (unsigned long long)(gridDim.x - 1));
+   }
+   __syncthreads();
+   if(!last)
+      return;
+   __threadfence();
+   kmin = ~0ULL; kmax = ~0ULL;
+   for(int i=threadIdx.x;i<(int)gridDim.x;i+=blockDim.x)
+   {
+      unsigned long long x = ((volatile unsigned long long *)part)[ 2*i ];
+      unsigned long long y = ((volatile unsigned long long *)part)[ 2*i+1 ];
+      kmin = x < kmin ? x : kmin;
+      kmax = y < kmax ? y : kmax;
+   }
+   for(int o=16;o>0;o>>=1)
+   {
+      unsigned long long x = __shfl_xor_sync(0xffffffffu, kmin, o);
+      unsigned long long y = __shfl_xor_sync(0xffffffffu, kmax, o);
+      kmin = x < kmin ? x : kmin;
+      kmax = y < kmax ? y : kmax;
+   }
+   if((threadIdx.x & 31) == 0)
+   {
+      shmin[ threadIdx.x >> 5 ] = kmin;
+      shmax[ threadIdx.x >> 5 ] = kmax;
+   }
+   __syncthreads();
+   if(threadIdx.x == 0)
+   {
+      for(int w=1;w<(int)(blockDim.x >> 5);w++)
+      {
+         kmin = shmin[w] < kmin ? shmin[w] : kmin;
+         kmax = shmax[w] < kmax ? shmax[w] : kmax;
+      }
+      scratch[1] = kmin;
+      scratch[2] = kmax;
+      *ticket = 0ULL;
+   }
+}
+
+static int red_blocks(GmdCtx *ctx, int n)
+{
+   int nb = (n + 4 * RED_THREADS - 1) / (4 * RED_THREADS);
+   int cap = 2 * gmd_num_sms(ctx);
+   if(nb > cap) nb = cap;
+   if(nb > RED_MAXBLK) nb = RED_MAXBLK;
+   if(nb < 1) nb = 1;
+   return nb;
+}
+
+extern "C" size_t gmd_reduce_scratch_bytes(int n)
+{
+   (void)n;
+   return (size_t)(3 + 2 * RED_MAXBLK) * sizeof(unsigned long long);
+}
+
+extern "C" int gmd_reduce_f32(GmdCtx *ctx, int op, const float *in, int n, double *res,
+                              void *scratch)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   unsigned long long *scr = (unsigned long long *)scratch;
+   int nb = red_blocks(ctx, n);
+
+   if(n <= 0)
+   {
+      *res = (op == 0) ? (double)FLT_MAX : (op == 1) ? -(double)FLT_MAX : 0.0;
+      return 1;
+   }
+
+   switch(op)
+   {
+      case 0: gml_reduce_f32_kernel<0><<<nb, RED_THREADS, 0, st>>>(in, n, scr); break;
+      case 1: gml_reduce_f32_kernel<1><<<nb, RED_THREADS, 0, st>>>(in, n, scr); break;
+      case 2: gml_reduce_f32_kernel<2><<<nb, RED_THREADS, 0, st>>>(in, n, scr); break;
+      case 3: gml_reduce_f32_kernel<3><<<nb, RED_THREADS, 0, st>>>(in, n, scr); break;
+      case 4: gml_reduce_f32_kernel<4><<<nb, RED_THREADS, 0, st>>>(in, n, scr); break;
+      case 5: gml_reduce_f32_kernel<5><<<nb, RED_THREADS, 0, st>>>(in, n, scr); break;
+      case 6: gml_reduce_f32_kernel<6><<<nb, RED_THREADS, 0, st>>>(in, n, scr); break;
+      default: return 0;
+   }
+   if(cudaGetLastError() != cudaSuccess)
+      return 0;
+   if(cudaMemcpyAsync(res, scr + 1, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return 0;
+   return cudaStreamSynchronize(st) == cudaSuccess;
+}
+
+extern "C" int gmd_minmax_arg_f32(GmdCtx *ctx, const float *in, int n,
+                                  float *vmin, int *imin, float *vmax, int *imax,
+                                  void *scratch)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   unsigned long long *scr = (unsigned long long *)scratch, host[2];
+   int nb = red_blocks(ctx, n);
+
+   if(n <= 0)
+      return 0;
+   gml_minmax_arg_kernel<<<nb, RED_THREADS, 0, st>>>(in, n, scr);
+   if(cudaGetLastError() != cudaSuccess)
+      return 0;
+   if(cudaMemcpyAsync(host, scr + 1, 2 * sizeof(unsigned long long),
+                      cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return 0;
+   if(cudaStreamSynchronize(st) != cudaSuccess)
+      return 0;
+   {
+      unsigned kmin = (unsigned)(host[0] >> 32), kmax = ~(unsigned)(host[1] >> 32);
+      unsigned umin = (kmin & 0x80000000u) ? (kmin & 0x7fffffffu) : ~kmin;
+      unsigned umax = (kmax & 0x80000000u) ? (kmax & 0x7fffffffu) : ~kmax;
+      float fmn, fmx;
+      memcpy(&fmn, &umin, 4);
+      memcpy(&fmx, &umax, 4);
+      if(vmin) *vmin = fmn;
+      if(imin) *imin = (int)(host[0] & 0xffffffffu);
+      if(vmax) *vmax = fmx;
+      if(imax) *imax = (int)(host[1] & 0xffffffffu);
+   }
+   return 1;
+}

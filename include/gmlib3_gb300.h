@@ -1,0 +1,134 @@
+/*
+ * gmlib3_gb300.h -- extensions of the GB300-native GMlib.
+ *
+ * Everything here is additive: gmlib3.h alone is the drop-in interface of the
+ * reference.  These entry points give foreign-function callers non-variadic
+ * forms of the variadic calls, expose the native mesh kernels, the solvers,
+ * the batched and served paths, and the controls of the launch machinery.
+ * Each declaration names the reference function it extends, or says that it
+ * has no counterpart in the reference.
+ */
+#ifndef GMLIB3_GB300_H
+#define GMLIB3_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "gmlib3.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------
+ * Instance control
+ * ------------------------------------------------------------------------- */
+
+/* Instance without a GPU: datatypes live in host memory, GmlCompileKernel
+   generates and compiles (NVRTC, sm_103a) but nothing can be launched.  For
+   checking generated kernels on machines without a GPU.  No counterpart in
+   the reference. */
+size_t   GmlxInitOffline      (void);
+
+/* 0 disables the per-launch CUDA events behind GmlGetKernelRunTime (needed
+   while capturing CUDA graphs by hand); 1 (default) enables them.  Extends
+   the reference's event recording of RunOclKrn (gmlib3.c:3207). */
+int      GmlxSetTiming        (size_t, int on);
+
+/* 0 disables block-size calibration (every generated kernel then uses
+   `block`, or 256 when block <= 0); 1 re-enables it.  Extends the reference's
+   work-group calibration (gmlib3.c:3142-3190). */
+int      GmlxSetTuning        (size_t, int on, int block);
+
+/* Block size chosen for a generated kernel (0 while still calibrating). */
+int      GmlxKernelBlockSize  (size_t, int KrnIdx);
+
+/* Generated CUDA source of a kernel (NULL for library kernels) and whether
+   its uplink gathers are lazy accessors (1) or eager arrays (0). */
+const char *GmlxKernelSource  (size_t, int KrnIdx);
+int      GmlxKernelIsLazy     (size_t, int KrnIdx);
+
+/* Number of 32-bit registers per thread of a generated kernel. */
+int      GmlxKernelRegisters  (size_t, int KrnIdx);
+
+/* 0: generated uplink gathers use the reference's eager per-thread arrays;
+   1 (default): lazy accessors, eager only when the body needs arrays. */
+int      GmlxSetLazy          (size_t, int on);
+
+/* Datatype indices of the link between two mesh types built by
+   GmlCompileKernel (base ball table, degree table, high-degree table; 0 when
+   absent).  Extends GmlGetLinkInfo (gmlib3.c:4307-4336). */
+int      GmlxLinkData         (size_t, int SrcTyp, int DstTyp, int *BalIdx, int *DegIdx,
+                               int *HghIdx);
+
+/* Wait for all work of the instance. */
+int      GmlxSynchronize      (size_t);
+
+/* CUDA stream (cudaStream_t) that orders all work of the instance. */
+void    *GmlxStream           (size_t);
+
+/* ---------------------------------------------------------------------------
+ * Non-variadic forms for foreign-function interfaces
+ * ------------------------------------------------------------------------- */
+
+/* GmlCompileKernel (gmlib3.c:2217) with the (index, flags, link) triplets
+   given as three arrays of NmbTyp entries. */
+int      GmlxCompileKernelV   (size_t, const char *src, const char *name, int MshTyp,
+                               int NmbTyp, const int *IdxTab, const int *FlgTab,
+                               const int *LnkTab);
+
+/* Whole-datatype copies between a caller buffer and a datatype, bytes equal
+   to the datatype size (lines x line size).  Set uploads (asynchronously),
+   Get downloads (blocking).  Bulk counterparts of GmlSetDataLine /
+   GmlGetDataLine (gmlib3.c:1841, 1910). */
+int      GmlxSetData          (size_t, int DatIdx, const void *buf, size_t bytes);
+int      GmlxGetData          (size_t, int DatIdx, void *buf, size_t bytes);
+
+/* Size in bytes, number of lines and device address of a datatype. */
+size_t   GmlxDataBytes        (size_t, int DatIdx);
+int      GmlxDataLines        (size_t, int DatIdx);
+void    *GmlxDevicePtr        (size_t, int DatIdx);
+
+/* ---------------------------------------------------------------------------
+ * Reductions with indices.  No counterpart in the reference (GmlReduceVector
+ * returns values only).  Ties go to the smallest line index.
+ * ------------------------------------------------------------------------- */
+int      GmlxReduceArg        (size_t, int DatIdx, float *MinVal, int *MinIdx,
+                               float *MaxVal, int *MaxIdx);
+
+/* ---------------------------------------------------------------------------
+ * Synthetic meshes and renumbering (host utilities).  No counterpart in the
+ * reference library; the reference renumbers meshes with an external Hilbert
+ * tool (README.md, todolist.md:44).
+ * ------------------------------------------------------------------------- */
+
+/* Unit cube of n^3 hexahedra split into 6 tetrahedra each.  split = 0: all
+   hexes split around the same main diagonal (Kuhn/Freudenthal, interior
+   vertex degree 24); split = 1: the diagonal of each hex goes through its
+   all-even corner (reflected split, ragged degrees 16/48).  Interior vertices
+   are jittered uniformly by +-jitter*h (h = 1/n) from a seed; boundary
+   vertices get reference 1, interior 0.  crd receives 4 floats per vertex
+   (w = 0), tet 4 ints per tetrahedron, ref one int per vertex.  Returns 1. */
+void     GmlxCubeSizes        (int n, int *NmbVer, int *NmbTet);
+int      GmlxCubeMesh         (int n, int split, double jitter, uint64_t seed,
+                               float *crd, int *tet, int *ref);
+
+/* Renumber vertices along a 3-D Hilbert curve of their coordinates and
+   tetrahedra along the curve of their centroids; arrays are permuted in
+   place.  VerPrm (optional) receives the new index of each old vertex. */
+int      GmlxHilbertRenumber  (int NmbVer, float *crd, int *ref, int NmbTet, int *tet,
+                               int *VerPrm);
+
+#ifdef __cplusplus
+}
+#endif
+
+/* internal helpers shared by the host files (not part of the public API) */
+#ifdef GML_INTERNAL_H
+const char *gmlx_intern(GmlSct *gml, const char *s);
+int      gmlx_cache_lookup(const char *src, const char *opts, const char *name, void **cubin, size_t *size);
+void     gmlx_cache_store(const char *src, const char *opts, const char *name, const void *cubin, size_t size);
+int      gmlx_timing_off(GmlSct *gml);
+void     gmlx_release_extensions(GmlSct *gml);
+#endif
+
+#endif

@@ -1,0 +1,172 @@
+"""Oracle: CPU restatement of the GMlib mesh-kernel path.
+
+TEST INFRASTRUCTURE.  Only tests/, __graft_entry__.smoke() and the CPU
+baseline leg of bench.py use it, as the checker.  The library never imports,
+links or calls anything here.
+
+  liboracle.so      C restatement (oracle.c, oracle_mesh.c), FP64
+  _ref/librefcl.so  the reference's kernel bodies compiled as C++, built only
+                    where the reference tree is present (see build.py)
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+_c = None
+_r = None
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def lib():
+    global _c
+    if _c is None:
+        _build.build_oracle()
+        _c = ctypes.CDLL(_build.LIB)
+        _c.orc_quality_ref1.restype = ctypes.c_double
+        _c.orc_mean_ratio1.restype = ctypes.c_double
+        _c.orc_det1.restype = ctypes.c_double
+        _c.orc_reduce.restype = ctypes.c_double
+        _c.orc_reduce.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    return _c
+
+
+def refcl():
+    """The reference's own kernel bodies on the CPU, or None where the
+    reference tree is absent."""
+    global _r
+    if _r is None:
+        path = _build.build_refcl()
+        if path is None:
+            return None
+        _r = ctypes.CDLL(path)
+    return _r
+
+
+# ------------------------------------------------------------------ wrappers
+
+def ver_tet_ball(nv, tet, bal_siz=32, max_siz=64, tables=True):
+    tet = np.ascontiguousarray(tet, np.int32)
+    nt = len(tet)
+    deg = np.zeros(nv, np.int32)
+    mp, hs = ctypes.c_int(), ctypes.c_int()
+    ok = lib().orc_ver_tet_ball(nv, nt, _ptr(tet), bal_siz, max_siz, _ptr(deg),
+                                ctypes.byref(mp), ctypes.byref(hs), None, None)
+    if not ok:
+        raise ValueError("degree above the maximum link width")
+    base = high = None
+    if tables:
+        base = np.zeros((mp.value + 1, bal_siz), np.int32)
+        high = np.zeros((max(nv - mp.value, 0), max(hs.value, 1)), np.int32)
+        lib().orc_ver_tet_ball(nv, nt, _ptr(tet), bal_siz, max_siz, _ptr(deg),
+                               ctypes.byref(mp), ctypes.byref(hs), _ptr(base),
+                               _ptr(high) if hs.value else None)
+        if not hs.value:
+            high = np.zeros((0, 0), np.int32)
+    return deg, mp.value, hs.value, base, high
+
+
+def tet_edges(tet):
+    tet = np.ascontiguousarray(tet, np.int32)
+    n = lib().orc_tet_edges(len(tet), _ptr(tet), None)
+    e = np.zeros((n, 2), np.int32)
+    lib().orc_tet_edges(len(tet), _ptr(tet), _ptr(e))
+    return e
+
+
+def quality_ref(crd, tet):
+    crd = np.ascontiguousarray(crd, np.float32)
+    tet = np.ascontiguousarray(tet, np.int32)
+    q = np.zeros(len(tet), np.float64)
+    lib().orc_quality_ref(len(tet), _ptr(crd), _ptr(tet), _ptr(q))
+    return q
+
+
+def mean_ratio(crd, tet):
+    crd = np.ascontiguousarray(crd, np.float32)
+    tet = np.ascontiguousarray(tet, np.int32)
+    q = np.zeros(len(tet), np.float64)
+    lib().orc_mean_ratio(len(tet), _ptr(crd), _ptr(tet), _ptr(q))
+    return q
+
+
+def reduce(op, x):
+    x = np.ascontiguousarray(x, np.float32)
+    return lib().orc_reduce(op, len(x), _ptr(x))
+
+
+def scatter(crd, tet):
+    crd = np.ascontiguousarray(crd, np.float32)
+    tet = np.ascontiguousarray(tet, np.int32)
+    opt = np.zeros((len(tet), 4, 4), np.float64)
+    lib().orc_scatter(len(tet), _ptr(crd), _ptr(tet), _ptr(opt))
+    return opt
+
+
+def gather(crd, deg, ball, opt):
+    crd = np.ascontiguousarray(crd, np.float32)
+    deg = np.ascontiguousarray(deg, np.int32)
+    ball = np.ascontiguousarray(ball, np.int32)
+    opt = np.ascontiguousarray(opt, np.float64)
+    nv = len(crd)
+    new = np.zeros((nv, 4), np.float64)
+    res = np.zeros(nv, np.float64)
+    lib().orc_gather(nv, _ptr(crd), _ptr(deg), _ptr(ball), ball.shape[1], _ptr(opt),
+                     _ptr(new), _ptr(res))
+    return new, res
+
+
+def ball_codes(nv, tet):
+    """Full vertex->tet ball (all entries, descending tet order) as a
+    (nv, maxdeg) table, built with the reference algorithm."""
+    deg, mp, hs, base, high = ver_tet_ball(nv, tet, 32, 64)
+    width = max(32, hs)
+    full = np.zeros((nv, width), np.int32)
+    full[:min(mp, nv), :32] = base[:min(mp, nv)]
+    if hs:
+        full[mp:, :hs] = high
+    return deg, full
+
+
+# --------------------------------------------------- reference bodies on CPU
+
+def ref_quality(crd, tet):
+    r = refcl()
+    if r is None:
+        return None
+    crd = np.ascontiguousarray(crd, np.float32)
+    tet = np.ascontiguousarray(tet, np.int32)
+    out = np.zeros(len(tet), np.float32)
+    r.ref_compute_quality(_ptr(crd), len(tet), _ptr(tet), _ptr(out))
+    return out
+
+
+def ref_scatter(crd, tet):
+    r = refcl()
+    if r is None:
+        return None
+    crd = np.ascontiguousarray(crd, np.float32)
+    tet = np.ascontiguousarray(tet, np.int32)
+    out = np.zeros((len(tet), 4, 4), np.float32)
+    r.ref_scatter(_ptr(crd), len(tet), _ptr(tet), _ptr(out))
+    return out
+
+
+def ref_gather(crd, deg, ball, opt):
+    r = refcl()
+    if r is None:
+        return None
+    crd = np.array(crd, np.float32, copy=True)
+    deg = np.ascontiguousarray(deg, np.int32)
+    ball = np.ascontiguousarray(ball, np.int32)
+    opt = np.ascontiguousarray(opt, np.float32)
+    res = np.zeros(len(crd), np.float32)
+    r.ref_gather(_ptr(crd), len(crd), _ptr(deg), _ptr(ball), ball.shape[1], _ptr(opt), _ptr(res))
+    return crd, res

@@ -1,0 +1,30 @@
+/*
+ * oracle.h -- CPU restatement of the GMlib mesh-kernel path (test
+ * infrastructure: the checker, never part of the library).
+ */
+#ifndef ORACLE_H
+#define ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+int    orc_ver_tet_ball(int nv, int nt, const int *tet, int BalSiz, int MaxSiz,
+                        int *deg, int *MaxPos, int *HghSiz, int *base, int *high);
+int    orc_tet_edges(int nt, const int *tet, int *edges);
+double orc_quality_ref1(const float *crd, const int *t);
+void   orc_quality_ref(int nt, const float *crd, const int *tet, double *q);
+double orc_mean_ratio1(const float *crd, const int *t);
+void   orc_mean_ratio(int nt, const float *crd, const int *tet, double *q);
+double orc_det1(const float *crd, const int *t);
+double orc_reduce(int op, int n, const float *x);
+void   orc_minmax_arg(int n, const double *x, double *vmin, int *imin, double *vmax, int *imax);
+void   orc_scatter(int nt, const float *crd, const int *tet, double *opt);
+void   orc_gather(int nv, const float *crd, const int *deg, const int *ball, int width,
+                  const double *opt, double *newcrd, double *res);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

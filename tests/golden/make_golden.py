@@ -1,0 +1,46 @@
+"""Generate tests/golden/*.npz from the reference's own kernel bodies.
+
+Runs where the reference tree is present: oracle/_ref/librefcl.so compiles
+sources/toolkit.cl and the MeshQuality / NodeSmoothing example bodies of the
+reference as C++ and executes them on the CPU (one loop iteration per
+work-item).  The fixtures store the inputs (a small jittered cube, Kuhn and
+reflected splits) and the reference outputs (quality, optimal points, relaxed
+coordinates, residuals) plus the ball tables built by the reference's chained
+hash algorithm (oracle.c).  Tests then pin the oracle and the GPU path to
+these values on machines without the reference tree.
+
+Usage:  python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+import gmlib_gb300 as G  # noqa: E402  (mesh generator only)
+import oracle as O  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def make(name, n, split, jitter, seed):
+    crd, tet, ref = G.cube_mesh(n, split=split, jitter=jitter, seed=seed)
+    deg, mp, hs, base, high = O.ver_tet_ball(len(crd), tet, 32, 64)
+    _, full = O.ball_codes(len(crd), tet)
+    q = O.ref_quality(crd, tet)
+    opt = O.ref_scatter(crd, tet)
+    newcrd, res = O.ref_gather(crd, deg, full, opt)
+    edges = O.tet_edges(tet)
+    np.savez_compressed(os.path.join(OUT, name), crd=crd, tet=tet, ref=ref, deg=deg,
+                        maxpos=mp, hghsiz=hs, base=base, high=high, quality=q, opt=opt,
+                        newcrd=newcrd, res=res, edges=edges)
+    print(name, len(crd), len(tet), "maxdeg", deg.max(), "maxpos", mp, "high", hs)
+
+
+if __name__ == "__main__":
+    if O.refcl() is None:
+        sys.exit("the reference tree is needed to generate the golden fixtures")
+    make("kuhn_n5.npz", 5, 0, 0.25, 12345)
+    make("reflected_n6.npz", 6, 1, 0.3, 777)

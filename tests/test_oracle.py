@@ -1,0 +1,109 @@
+"""The oracle against the golden fixtures made from the reference's own
+kernel bodies, and against hand-derived known answers."""
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = ["kuhn_n5.npz", "reflected_n6.npz"]
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLD, name)))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_quality_matches_reference_bodies(O, case):
+    g = load(case)
+    q = O.quality_ref(g["crd"], g["tet"])
+    # the fixture is the reference body evaluated in FP32 on the CPU
+    assert np.max(np.abs(q - g["quality"])) <= 1e-6 * np.max(np.abs(q))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_scatter_gather_match_reference_bodies(O, case):
+    g = load(case)
+    opt = O.scatter(g["crd"], g["tet"])
+    assert np.max(np.abs(opt - g["opt"])) <= 1e-6
+    deg, full = O.ball_codes(len(g["crd"]), g["tet"])
+    new, res = O.gather(g["crd"], deg, full, opt)
+    assert np.max(np.abs(new - g["newcrd"])) <= 1e-6
+    assert np.max(np.abs(res - g["res"])) <= 1e-7
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_ball_tables_are_stable(O, case):
+    """Integer tables: bit-exact against the fixture (reference algorithm)."""
+    g = load(case)
+    deg, mp, hs, base, high = O.ver_tet_ball(len(g["crd"]), g["tet"], 32, 64)
+    assert np.array_equal(deg, g["deg"])
+    assert mp == int(g["maxpos"]) and hs == int(g["hghsiz"])
+    assert np.array_equal(base, g["base"])
+    assert np.array_equal(high, g["high"])
+    assert np.array_equal(O.tet_edges(g["tet"]), g["edges"])
+
+
+def test_ball_known_answer(O):
+    """Two tets sharing face (1,2,3): the ball lists elements in descending
+    index order with codes (element << 4) | local index."""
+    tet = np.array([[0, 1, 2, 3], [4, 3, 2, 1]], np.int32)
+    deg, mp, hs, base, high = O.ver_tet_ball(5, tet, 32, 64)
+    assert deg.tolist() == [1, 2, 2, 2, 1]
+    assert mp == 5 and hs == 0
+    assert base[0, :1].tolist() == [(0 << 4) | 0]
+    assert base[1, :2].tolist() == [(1 << 4) | 3, (0 << 4) | 1]
+    assert base[2, :2].tolist() == [(1 << 4) | 2, (0 << 4) | 2]
+    assert base[3, :2].tolist() == [(1 << 4) | 1, (0 << 4) | 3]
+    assert base[4, :1].tolist() == [(1 << 4) | 0]
+    assert not base[0, 1:].any()
+
+
+def test_edges_known_answer(O):
+    """Edges in order of first appearance, local order (0,1) (1,2) (2,0)
+    (3,0) (3,1) (3,2), stored (min, max)."""
+    tet = np.array([[0, 1, 2, 3], [4, 3, 2, 1]], np.int32)
+    e = O.tet_edges(tet).tolist()
+    assert e == [[0, 1], [1, 2], [0, 2], [0, 3], [1, 3], [2, 3], [3, 4], [2, 4], [1, 4]]
+
+
+def test_high_degree_split(O):
+    """Reflected split: degrees up to 48 need the 64-wide high table; line
+    MaxPos is the first line above 32 and its full ball is in high row 0."""
+    g = load("reflected_n6.npz")
+    deg, mp, hs, base, high = O.ver_tet_ball(len(g["crd"]), g["tet"], 32, 64)
+    assert hs == 64
+    assert deg[:mp].max() <= 32 and deg[mp] > 32
+    codes = high[0, :deg[mp]]
+    assert np.all(np.diff(codes >> 4) < 0)          # descending elements
+    assert not high[0, deg[mp]:].any()
+    assert np.array_equal(base[mp], high[0, :32])
+
+
+@pytest.mark.parametrize("op", range(7))
+def test_reduce_known_answers(O, op):
+    x = np.array([3.0, -1.5, 0.0, 2.25, -4.0], np.float32)
+    expect = [-4.0, 3.0, -0.25, 4.0, 10.75, 9 + 2.25 + 5.0625 + 16, 4.0][op]
+    assert O.reduce(op, x) == pytest.approx(expect, abs=1e-12)
+
+
+def test_mean_ratio_regular_tet(O):
+    s = np.sqrt(2.0)
+    crd = np.array([[1, 0, -1 / s, 0], [-1, 0, -1 / s, 0], [0, 1, 1 / s, 0], [0, -1, 1 / s, 0]],
+                   np.float32)
+    tet = np.array([[0, 1, 2, 3]], np.int32)
+    q = O.mean_ratio(crd, tet)
+    assert abs(abs(q[0]) - 1.0) < 1e-6
+    q2 = O.mean_ratio(crd, tet[:, [0, 2, 1, 3]])
+    assert q2[0] == pytest.approx(-q[0])
+
+
+def test_refcl_fresh_mesh(O, G):
+    """Where the reference tree is present, its bodies and the oracle agree
+    on a mesh that is not in the fixtures."""
+    if O.refcl() is None:
+        pytest.skip("reference tree not present")
+    crd, tet, ref = G.cube_mesh(7, split=1, jitter=0.3, seed=99)
+    q = O.quality_ref(crd, tet)
+    qr = O.ref_quality(crd, tet)
+    assert np.max(np.abs(q - qr)) <= 1e-6 * np.max(np.abs(q))
