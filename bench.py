@@ -1,0 +1,386 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 GMlib mesh-kernel path.
+
+Workload (one "step"): the smoothing configuration on a 128^3-hex unit cube
+split into 6 tets per hex with the reflected split (12,582,912 tets,
+2,146,689 vertices, ragged vertex->tet degrees 4..48), interior vertices
+jittered by +-0.3h, Hilbert renumbered, boundary vertices fixed: 10 Jacobi
+sweeps of Laplacian smoothing over the ball of points, each followed by the
+mean-ratio quality of every tet with a 64-bin histogram, min/argmin and
+FP64-decided inverted-element flags.  One step is one replay of the CUDA
+graph built by GmlxSmoothQualityLoop.
+
+value      algorithmic (unique) bytes of a step / device time of a step, GB/s,
+           inputs resident in HBM; timed with CUDA events on the library's
+           stream over K steps after W warm-up steps.
+e2e        the same bytes / wall time of a step through the C ABI with host
+           buffers: upload of the coordinates (pinned host mirror), the step,
+           download of the statistics and of the coordinates.
+roofline   the dominant kernel, its algorithmic bytes per launch / its mean
+           launch time measured here with CUDA events, against the measured
+           HBM copy bandwidth.
+cpu_baseline  the oracle's multithreaded port of the same workload on the
+           host cores (a bounded sample: one sweep + one quality pass).
+
+--impl reference times that CPU port as the reference arm (the reference
+itself is OpenCL and has no runnable CPU path here).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_HEX = 128
+SPLIT = 1
+JITTER = 0.3
+SEED = 2024
+SWEEPS = 10
+OMEGA = 1.0
+FALLBACK_HBM = 6800.0
+METRIC = "HBM GB/s/kernel"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=600)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n", type=int, default=N_HEX, help="hexes per cube side")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--e2e-steps", type=int, default=20)
+    return p.parse_args()
+
+
+# --------------------------------------------------------------- distributed
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# -------------------------------------------------------------------- clocks
+
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(self.dev)],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, val in zip(names, parts[5:9]):
+                    if val.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ----------------------------------------------------------------- helpers
+
+def peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, burst copy)"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM, "fallback 6.8 TB/s"
+
+
+def traffic_for(kernel):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d.get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def mesh(n):
+    import gmlib_gb300 as G
+    crd, tet, ref = G.cube_mesh(n, split=SPLIT, jitter=JITTER, seed=SEED)
+    return crd, tet, ref
+
+
+def workload_config(n, nv, nt, wset_mb):
+    return {"workload": "ball-of-points Laplacian smoothing + mean-ratio quality, "
+                        "%d^3-hex cube, reflected 6-tet split" % n,
+            "hex_per_side": n, "tets": nt, "vertices": nv, "sweeps_per_step": SWEEPS,
+            "per_sweep": "Jacobi sweep (boundary fixed) + quality, 64-bin histogram, "
+                         "min/argmin, FP64 inverted flags",
+            "jitter": JITTER, "seed": SEED, "omega": OMEGA,
+            "l2": "inputs larger than L2: %.0f MB working set > 129 MB L2" % wset_mb}
+
+
+# ---------------------------------------------------------------- CPU port
+
+def cpu_port(crd, tet, ref, nsweeps, reps):
+    """Time the oracle's OpenMP port: nsweeps sweep+quality passes, reps
+    times; returns (seconds per pass list, threads)."""
+    import oracle as O
+    lib = O.lib()
+    fixed = (ref != 0).astype(np.int32)
+    ptr, col = O.point_ball(len(crd), tet, fixed)
+    c = np.array(crd, np.float32, copy=True)
+    tmp = np.zeros_like(c)
+    hist = np.zeros(64 * nsweeps, np.uint32)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        lib.orc_bench_step(len(c), len(tet), O._ptr(c), O._ptr(tmp), O._ptr(tet), O._ptr(ptr),
+                           O._ptr(col), ctypes.c_float(OMEGA), nsweeps, O._ptr(hist), None,
+                           None, None)
+        ts.append((time.perf_counter() - t0) / nsweeps)
+    return ts, lib.orc_threads(), len(col)
+
+
+def step_bytes_host(nv, nt, used):
+    sweep = 4.0 * nv + 4.0 * used + 32.0 * nv
+    qual = 16.0 * nt + 16.0 * nv + 4.0 * ((nt + 31) // 32)
+    return sweep, qual
+
+
+# ------------------------------------------------------------- reference arm
+
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return
+    n = args.n
+    crd, tet, ref = mesh(n)
+    steps = min(args.steps, 20)
+    warm = min(args.warmup, 3)
+    ts, threads, used = cpu_port(crd, tet, ref, 1, warm + steps)
+    ts = ts[warm:]
+    sweep, qual = step_bytes_host(len(crd), len(tet), used)
+    per = statistics.median(ts)
+    value = (sweep + qual) / per / 1e9
+    wset = (16.0 * len(tet) + 32.0 * len(crd) + 4.0 * used) / 1e6
+    sample = ("one sweep + one quality pass (1/%d of a step) on the full mesh per timed "
+              "step, %d timed steps" % (SWEEPS, steps))
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+            "ms_per_step": round(per * SWEEPS * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(n, len(crd), len(tet), wset),
+            "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference is OpenCL host code plus OpenCL kernels; no OpenCL "
+                    "runtime exists on this box, so its CPU path is the oracle's "
+                    "OpenMP port of the same workload"}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def run_gpu(args, dist):
+    import gmlib_gb300 as G
+    n = args.n
+    h = 1.0 / n
+    dev = dist.local
+    crd, tet, ref = mesh(n)
+    nv, nt = len(crd), len(tet)
+
+    g = G.lib.GmlInit(dev)
+    if not g:
+        raise SystemExit("GmlInit(%d) failed" % dev)
+    G.lib.GmlxSetTiming(g, 0)
+    vidx, tidx = G.upload_mesh(g, crd, tet, ref)
+    if G.lib.GmlxMeshSetup(g, 1) != 1:
+        raise SystemExit("GmlxMeshSetup failed")
+    sweep_b, qual_b = ctypes.c_double(), ctypes.c_double()
+    G.lib.GmlxMeshBytes(g, ctypes.byref(sweep_b), ctypes.byref(qual_b))
+    step_bytes = SWEEPS * (sweep_b.value + qual_b.value)
+    stored, used, mx = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
+    G.lib.GmlxMeshBallInfo(g, ctypes.byref(stored), ctypes.byref(used), ctypes.byref(mx))
+    wset = (16.0 * nt + 32.0 * nv + 4.0 * stored.value) / 1e6
+    res = (G.GmlxQuality * SWEEPS)()
+    om = ctypes.c_float(OMEGA)
+
+    for _ in range(args.warmup):
+        G.lib.GmlxSmoothQualityLoop(g, SWEEPS, om, h, None)
+    G.lib.GmlxSynchronize(g)
+
+    e0, e1 = G.lib.GmlxEventCreate(), G.lib.GmlxEventCreate()
+    clocks = Clocks(dev)
+    dist.barrier()
+    G.lib.GmlxSynchronize(g)
+    clocks.start()
+    time.sleep(0.3)
+    G.lib.GmlxEventRecord(g, e0)
+    for _ in range(args.steps):
+        if G.lib.GmlxSmoothQualityLoop(g, SWEEPS, om, h, None) != 1:
+            raise SystemExit("step failed")
+    G.lib.GmlxEventRecord(g, e1)
+    dev_s = G.lib.GmlxEventElapsed(e0, e1)
+    G.lib.GmlxSynchronize(g)
+    clk = clocks.stop()
+    dist.barrier()
+    dev_s = dist.max(dev_s)
+    per_step = dev_s / args.steps
+    value = dist.world * step_bytes / per_step / 1e9
+
+    # statistics of the last step (checks that the step did its work)
+    G.lib.GmlxSmoothQualityLoop(g, SWEEPS, om, h, res)
+    last = res[SWEEPS - 1]
+
+    # per-kernel launch times, same stream, CUDA events
+    reps = 50
+    G.lib.GmlxEventRecord(g, e0)
+    for _ in range(reps):
+        G.lib.GmlxSmooth(g, 2, om)
+    G.lib.GmlxEventRecord(g, e1)
+    t_sweep = G.lib.GmlxEventElapsed(e0, e1) / (2 * reps)
+    G.lib.GmlxEventRecord(g, e0)
+    for _ in range(reps):
+        G.lib.GmlxQualityStats(g, h, 0, None)
+    G.lib.GmlxEventRecord(g, e1)
+    t_qual = G.lib.GmlxEventElapsed(e0, e1) / reps
+    peak, peak_src = peak_hbm()
+    kern = [("laplace_sell_kernel", sweep_b.value, t_sweep),
+            ("tet_quality_kernel", qual_b.value, t_qual)]
+    kern.sort(key=lambda k: -k[2])
+    name, kb, kt = kern[0]
+    achieved = kb / kt / 1e9
+    roof = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic_for(name),
+            "algorithmic_bytes_per_launch": kb, "mean_launch_us": round(kt * 1e6, 2),
+            "peak_source": peak_src,
+            "other_kernels": [{"kernel": k[0], "achieved": round(k[1] / k[2] / 1e9, 1),
+                               "frac": round(k[1] / k[2] / 1e9 / peak, 4),
+                               "mean_launch_us": round(k[2] * 1e6, 2)} for k in kern[1:]]}
+
+    # end to end through the C ABI with host buffers
+    host_crd = np.ascontiguousarray(crd)
+    out_crd = np.empty_like(host_crd)
+    e2e_t = []
+    for i in range(args.e2e_steps + 2):
+        t0 = time.perf_counter()
+        G.lib.GmlxSetData(g, vidx, G.as_ptr(host_crd), host_crd.nbytes)
+        G.lib.GmlxSmoothQualityLoop(g, SWEEPS, om, h, res)
+        G.lib.GmlxGetData(g, vidx, G.as_ptr(out_crd), out_crd.nbytes)
+        if i >= 2:
+            e2e_t.append(time.perf_counter() - t0)
+    e2e_s = dist.max(statistics.median(e2e_t))
+    e2e = {"value": round(dist.world * step_bytes / e2e_s / 1e9, 3), "unit": "GB/s",
+           "h2d_bytes_per_step": host_crd.nbytes,
+           "d2h_bytes_per_step": out_crd.nbytes + SWEEPS * ctypes.sizeof(G.GmlxQuality),
+           "ms_per_step": round(e2e_s * 1e3, 3)}
+
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        ts, threads, cused = cpu_port(crd, tet, ref, 1, 3)
+        sw, qu = step_bytes_host(nv, nt, cused)
+        cpu = {"value": round((sw + qu) / statistics.median(ts) / 1e9, 3), "unit": "GB/s",
+               "cores": threads, "kind": "port",
+               "sample": "one sweep + one quality pass (1/%d of a step) on the full mesh, "
+                         "median of 3" % SWEEPS}
+
+    G.lib.GmlStop(g)
+
+    if dist.rank == 0:
+        line = {"metric": METRIC, "value": round(value, 3), "unit": "GB/s",
+                "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": round(per_step * 1e3, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": workload_config(n, nv, nt, wset),
+                "gpu_launches": args.steps * (2 * SWEEPS + 1),
+                "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
+                "result_check": {"last_sweep_min_quality": last.MinQal,
+                                 "last_sweep_argmin": last.MinIdx,
+                                 "inverted": last.NmbInv, "fp64_determinants": last.NmbF64,
+                                 "ball_entries_used": used.value,
+                                 "ball_entries_stored": stored.value,
+                                 "max_ball_of_points": mx.value}}
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_gpu(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -102,6 +102,30 @@ SIGNATURES = {
 }
 
 
+class GmlxQuality(ctypes.Structure):
+    _fields_ = [("MinQal", ctypes.c_float), ("MaxQal", ctypes.c_float),
+                ("MinIdx", ctypes.c_int), ("MaxIdx", ctypes.c_int),
+                ("SumQal", ctypes.c_double), ("NmbInv", ctypes.c_uint),
+                ("NmbF64", ctypes.c_uint), ("Hist", ctypes.c_uint * 64)]
+
+
+_qp = ctypes.POINTER(GmlxQuality)
+_llp = ctypes.POINTER(ctypes.c_longlong)
+SIGNATURES.update({
+    "GmlxMeshSetup": (_i, [_s, _i]),
+    "GmlxMeshBallInfo": (_i, [_s, _llp, _llp, _ip]),
+    "GmlxSmooth": (_i, [_s, _i, _f]),
+    "GmlxQualityStats": (_i, [_s, _d, _i, _qp]),
+    "GmlxInvertedFlags": (_i, [_s, _p, _s]),
+    "GmlxSmoothQualityLoop": (_i, [_s, _i, _f, _d, _qp]),
+    "GmlxMeshBytes": (_i, [_s, _dp, _dp]),
+    "GmlxEventCreate": (_p, []),
+    "GmlxEventRecord": (_i, [_s, _p]),
+    "GmlxEventElapsed": (_d, [_p, _p]),
+    "GmlxEventDestroy": (None, [_p]),
+})
+
+
 def _load():
     if not os.path.exists(LIB_PATH):
         raise ImportError("libgmlib3.so is not built: run `python -m gmlib_gb300.build` "

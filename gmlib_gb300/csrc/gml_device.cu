@@ -396,6 +396,50 @@ extern "C" void gmd_module_unload(void *module)
       p_cuModuleUnload((CUmodule)module);
 }
 
+/* ------------------------------------------------------------------------- */
+/* CUDA graphs                                                                */
+/* ------------------------------------------------------------------------- */
+
+extern "C" int gmd_graph_begin(GmdCtx *ctx)
+{
+   if(!ctx)
+      return 0;
+   return ok(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal),
+             "begin graph capture");
+}
+
+extern "C" int gmd_graph_end(GmdCtx *ctx, void **exec)
+{
+   cudaGraph_t g = NULL;
+   cudaGraphExec_t e = NULL;
+   *exec = NULL;
+   if(!ctx)
+      return 0;
+   if(!ok(ctx, cudaStreamEndCapture(ctx->stream, &g), "end graph capture"))
+      return 0;
+   if(!ok(ctx, cudaGraphInstantiate(&e, g, 0), "graph instantiate"))
+   {
+      cudaGraphDestroy(g);
+      return 0;
+   }
+   cudaGraphDestroy(g);
+   *exec = (void *)e;
+   return 1;
+}
+
+extern "C" int gmd_graph_launch(GmdCtx *ctx, void *exec)
+{
+   if(!ctx || !exec)
+      return 0;
+   return ok(ctx, cudaGraphLaunch((cudaGraphExec_t)exec, ctx->stream), "graph launch");
+}
+
+extern "C" void gmd_graph_free(void *exec)
+{
+   if(exec)
+      cudaGraphExecDestroy((cudaGraphExec_t)exec);
+}
+
 extern "C" int gmd_launch(GmdCtx *ctx, void *func, unsigned grid, unsigned block,
                           unsigned smem, void **args)
 {

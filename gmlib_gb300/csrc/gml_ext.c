@@ -257,6 +257,15 @@ void *GmlxStream(size_t GmlIdx)
    return gmd_stream(gml->dev);
 }
 
+void *GmlxEventCreate(void)              { return gmd_event_new(); }
+int GmlxEventRecord(size_t GmlIdx, void *evt)
+{
+   GETGMLPTR(gml, GmlIdx);
+   return gmd_event_record(gml->dev, evt);
+}
+double GmlxEventElapsed(void *beg, void *end) { return gmd_event_elapsed_s(beg, end); }
+void GmlxEventDestroy(void *evt)         { gmd_event_free(evt); }
+
 /* ========================================================================= */
 /* non-variadic forms                                                         */
 /* ========================================================================= */

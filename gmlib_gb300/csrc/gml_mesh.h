@@ -1,0 +1,41 @@
+/*
+ * gml_mesh.h -- device entry points of the native mesh kernels
+ * (gml_mesh_kernels.cu), called by gml_native.c.
+ */
+#ifndef GML_MESH_H
+#define GML_MESH_H
+
+#include "gmlib3_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+struct GmdCtx;
+
+int gmd_mesh_vt_csr(struct GmdCtx *ctx, const void *tet, int nt, int nv,
+                    int *ptr, int *vt, int *tmp, int *err);
+int gmd_mesh_boundary(struct GmdCtx *ctx, const void *tet, int nt, const int *ptr,
+                      const int *vt, int *fixed);
+int gmd_mesh_point_count(struct GmdCtx *ctx, const void *tet, int nv, const int *ptr,
+                         const int *vt, const int *fixed, int *pdeg,
+                         long long *width, long long *soff, int *err);
+int gmd_mesh_point_fill(struct GmdCtx *ctx, const void *tet, int nv, const int *ptr,
+                        const int *vt, const int *pdeg, const long long *soff, int *pcol);
+int gmd_mesh_laplace(struct GmdCtx *ctx, int nv, const long long *soff, const int *pdeg,
+                     const int *pcol, const void *in, void *out, float omega);
+int gmd_mesh_stats_init(struct GmdCtx *ctx, GmlxQualStats *st, int n);
+int gmd_mesh_quality(struct GmdCtx *ctx, int nt, const void *tet, const void *crd, float thr,
+                     float *qout, unsigned *flags, GmlxQualStats *st);
+
+/* CUDA graphs on the instance stream */
+int  gmd_graph_begin(struct GmdCtx *ctx);
+int  gmd_graph_end(struct GmdCtx *ctx, void **exec);
+int  gmd_graph_launch(struct GmdCtx *ctx, void *exec);
+void gmd_graph_free(void *exec);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,12 +1,389 @@
 /*
  * gml_native.c -- host side of the native mesh kernels (no counterpart in the
- * reference API).  Filled in by the native smoothing / quality extensions.
+ * reference API): topology setup, Laplacian smoothing over the ball of
+ * points, mean-ratio quality statistics, and the smoothing workload captured
+ * as a CUDA graph.
  */
+#include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 #include "gml_internal.h"
 #include "gmlib3_gb300.h"
+#include "gml_mesh.h"
+
+typedef struct
+{
+   int         nv, nt, fix, ready;
+   int         *ptr, *vt, *tmp, *err, *fixed, *pdeg, *pcol;
+   long long   *width, *soff;
+   long long   ncol, used;
+   int         maxdeg;
+   void        *crd2;                 /* second coordinate buffer */
+   unsigned    *flags;                /* inverted-element bits */
+   GmlxQualStats *stats;              /* device, GML_MAXSTATS entries */
+   int         nstats;
+   void        *graph;                /* smoothing workload graph */
+   int         gsweeps;
+   float       gomega;
+   double      gh;
+   void        *gver, *gtet;          /* buffers the graph was captured on */
+   int         NmbLoopKrn, NmbSweepKrn, NmbQalKrn;
+}NatSct;
+
+#define GML_MAXSTATS 64
+
+static NatSct *nat(GmlSct *gml)
+{
+   if(!gml->ext)
+      gml->ext = calloc(1, sizeof(NatSct));
+   return (NatSct *)gml->ext;
+}
+
+static void free_state(GmlSct *gml, NatSct *n)
+{
+   gmd_sync(gml->dev);
+   gmd_free(gml->dev, n->ptr);   gmd_free(gml->dev, n->vt);
+   gmd_free(gml->dev, n->tmp);   gmd_free(gml->dev, n->err);
+   gmd_free(gml->dev, n->fixed); gmd_free(gml->dev, n->pdeg);
+   gmd_free(gml->dev, n->pcol);  gmd_free(gml->dev, n->width);
+   gmd_free(gml->dev, n->soff);  gmd_free(gml->dev, n->crd2);
+   gmd_free(gml->dev, n->flags); gmd_free(gml->dev, n->stats);
+   gmd_graph_free(n->graph);
+   memset(n, 0, sizeof(NatSct));
+}
 
 void gmlx_native_release(GmlSct *gml)
 {
-   (void)gml;
+   if(gml->ext)
+   {
+      free_state(gml, (NatSct *)gml->ext);
+      free(gml->ext);
+      gml->ext = NULL;
+   }
+}
+
+static int mesh_dat(GmlSct *gml, GmlDatSct **ver, GmlDatSct **tet)
+{
+   if(!gml->TypIdx[ GmlVertices ] || !gml->TypIdx[ GmlTetrahedra ])
+   {
+      puts("The native mesh kernels need vertices and tetrahedra.");
+      return 0;
+   }
+   *ver = &gml->dat[ gml->TypIdx[ GmlVertices ] ];
+   *tet = &gml->dat[ gml->TypIdx[ GmlTetrahedra ] ];
+   return 1;
+}
+
+int GmlxMeshSetup(size_t GmlIdx, int fix)
+{
+   GETGMLPTR(gml, GmlIdx);
+   GmlDatSct *ver, *tet;
+   NatSct *n;
+   int nv, nt, err = 0, ns, *pdeg_h;
+   long long *soff_h;
+
+   if(gml->Offline || !mesh_dat(gml, &ver, &tet))
+      return 0;
+
+   n = nat(gml);
+   free_state(gml, n);
+   nv = ver->NmbLin;
+   nt = tet->NmbLin;
+   ns = (nv + 31) / 32;
+   n->nv = nv;
+   n->nt = nt;
+   n->fix = fix;
+
+   n->ptr   = gmd_alloc(gml->dev, (size_t)(nv + 1) * sizeof(int));
+   n->vt    = gmd_alloc(gml->dev, (size_t)nt * 4 * sizeof(int));
+   n->tmp   = gmd_alloc(gml->dev, (size_t)nv * sizeof(int));
+   n->err   = gmd_alloc(gml->dev, sizeof(int));
+   n->pdeg  = gmd_alloc(gml->dev, (size_t)nv * sizeof(int));
+   n->width = gmd_alloc(gml->dev, (size_t)(ns + 1) * sizeof(long long));
+   n->soff  = gmd_alloc(gml->dev, (size_t)(ns + 1) * sizeof(long long));
+   n->crd2  = gmd_alloc(gml->dev, (size_t)nv * 16);
+   n->flags = gmd_alloc(gml->dev, (size_t)((nt + 31) / 32) * sizeof(unsigned));
+   n->stats = gmd_alloc(gml->dev, GML_MAXSTATS * sizeof(GmlxQualStats));
+   n->nstats = GML_MAXSTATS;
+   if(!n->ptr || !n->vt || !n->tmp || !n->err || !n->pdeg || !n->width || !n->soff
+   || !n->crd2 || !n->flags || !n->stats)
+   {
+      free_state(gml, n);
+      return 0;
+   }
+
+   if(!gmd_mesh_vt_csr(gml->dev, tet->GpuMem, nt, nv, n->ptr, n->vt, n->tmp, n->err))
+   {
+      free_state(gml, n);
+      return 0;
+   }
+
+   if(fix == 1)
+   {
+      /* vertices with a non-zero reference are fixed */
+      int *ref = (int *)gml->dat[ gml->RefIdx[ GmlVertices ] ].CpuMem, i;
+      int *fx = malloc((size_t)nv * sizeof(int));
+      if(!fx) { free_state(gml, n); return 0; }
+      gml_wait_upload(gml, &gml->dat[ gml->RefIdx[ GmlVertices ] ]);
+      for(i=0;i<nv;i++)
+         fx[i] = ref && ref[i] != 0;
+      n->fixed = gmd_alloc(gml->dev, (size_t)nv * sizeof(int));
+      gmd_h2d_async(gml->dev, n->fixed, fx, (size_t)nv * sizeof(int));
+      gmd_sync(gml->dev);
+      free(fx);
+   }
+   else if(fix == 2)
+   {
+      n->fixed = gmd_alloc(gml->dev, (size_t)nv * sizeof(int));
+      gmd_mesh_boundary(gml->dev, tet->GpuMem, nt, n->ptr, n->vt, n->fixed);
+   }
+
+   gmd_mesh_point_count(gml->dev, tet->GpuMem, nv, n->ptr, n->vt, n->fixed, n->pdeg,
+                        n->width, n->soff, n->err);
+
+   soff_h = malloc((size_t)(ns + 1) * sizeof(long long));
+   pdeg_h = malloc((size_t)nv * sizeof(int));
+   if(!soff_h || !pdeg_h)
+   {
+      free(soff_h); free(pdeg_h);
+      free_state(gml, n);
+      return 0;
+   }
+   gmd_d2h(gml->dev, &err, n->err, sizeof(int));
+   gmd_d2h(gml->dev, soff_h, n->soff, (size_t)(ns + 1) * sizeof(long long));
+   gmd_d2h(gml->dev, pdeg_h, n->pdeg, (size_t)nv * sizeof(int));
+
+   if(err)
+   {
+      printf("GmlxMeshSetup: %s\n", (err & 2) ? "vertex index out of range in the tetrahedra"
+                                               : "a ball of points exceeds 64 vertices");
+      free(soff_h); free(pdeg_h);
+      free_state(gml, n);
+      return 0;
+   }
+
+   n->ncol = soff_h[ns];
+   n->used = 0;
+   n->maxdeg = 0;
+   for(int i=0;i<nv;i++)
+   {
+      n->used += pdeg_h[i];
+      if(pdeg_h[i] > n->maxdeg) n->maxdeg = pdeg_h[i];
+   }
+   free(soff_h);
+   free(pdeg_h);
+
+   n->pcol = gmd_alloc(gml->dev, (size_t)(n->ncol > 0 ? n->ncol : 1) * 32 * sizeof(int));
+   if(!n->pcol)
+   {
+      free_state(gml, n);
+      return 0;
+   }
+   gmd_mesh_point_fill(gml->dev, tet->GpuMem, nv, n->ptr, n->vt, n->pdeg, n->soff, n->pcol);
+   gmd_sync(gml->dev);
+   n->ready = 1;
+   return 1;
+}
+
+int GmlxMeshBallInfo(size_t GmlIdx, long long *stored, long long *used, int *maxdeg)
+{
+   GETGMLPTR(gml, GmlIdx);
+   NatSct *n = gml->ext;
+   if(!n || !n->ready)
+      return 0;
+   if(stored) *stored = n->ncol * 32;
+   if(used) *used = n->used;
+   if(maxdeg) *maxdeg = n->maxdeg;
+   return 1;
+}
+
+static int ready(GmlSct *gml, NatSct **n, GmlDatSct **ver, GmlDatSct **tet)
+{
+   *n = gml->ext;
+   if(!*n || !(*n)->ready)
+   {
+      puts("GmlxMeshSetup must be called first.");
+      return 0;
+   }
+   if(!mesh_dat(gml, ver, tet))
+      return 0;
+   if((*ver)->NmbLin != (*n)->nv || (*tet)->NmbLin != (*n)->nt)
+   {
+      puts("The mesh changed since GmlxMeshSetup.");
+      return 0;
+   }
+   return 1;
+}
+
+/* sweeps alternate between the vertex buffer and a second buffer; an odd
+   count ends with a copy back */
+static int sweeps(GmlSct *gml, NatSct *n, GmlDatSct *ver, int ns, float omega)
+{
+   void *a = ver->GpuMem, *b = n->crd2;
+   for(int s=0;s<ns;s++)
+   {
+      if(!gmd_mesh_laplace(gml->dev, n->nv, n->soff, n->pdeg, n->pcol, a, b, omega))
+         return 0;
+      void *t = a; a = b; b = t;
+   }
+   if(a != ver->GpuMem)
+      gmd_d2d_async(gml->dev, ver->GpuMem, a, (size_t)n->nv * 16);
+   return 1;
+}
+
+int GmlxSmooth(size_t GmlIdx, int nsweeps, float omega)
+{
+   GETGMLPTR(gml, GmlIdx);
+   NatSct *n;
+   GmlDatSct *ver, *tet;
+   if(!ready(gml, &n, &ver, &tet) || nsweeps < 0)
+      return 0;
+   if(!n->NmbSweepKrn)
+      n->NmbSweepKrn = gml_new_kernel_slot(gml, GmlKrnGenerated + 100, "laplace_sell");
+   gml_lib_timer_begin(gml, &gml->krn[ n->NmbSweepKrn ]);
+   if(!sweeps(gml, n, ver, nsweeps, omega))
+      return 0;
+   gml_lib_timer_end(gml, &gml->krn[ n->NmbSweepKrn ]);
+   return 1;
+}
+
+static void decode(const GmlxQualStats *s, GmlxQuality *r)
+{
+   unsigned kmin = (unsigned)(s->MinKey >> 32), kmax = ~(unsigned)(s->MaxKey >> 32);
+   unsigned umin = (kmin & 0x80000000u) ? (kmin & 0x7fffffffu) : ~kmin;
+   unsigned umax = (kmax & 0x80000000u) ? (kmax & 0x7fffffffu) : ~kmax;
+   memcpy(&r->MinQal, &umin, 4);
+   memcpy(&r->MaxQal, &umax, 4);
+   r->MinIdx = (int)(s->MinKey & 0xffffffffu);
+   r->MaxIdx = (int)(s->MaxKey & 0xffffffffu);
+   r->SumQal = s->Sum;
+   r->NmbInv = s->NmbInv;
+   r->NmbF64 = s->NmbF64;
+   memcpy(r->Hist, s->Hist, sizeof(r->Hist));
+}
+
+static float det_threshold(double h)
+{
+   return (float)(1e-6 * h * h * h);
+}
+
+int GmlxQualityStats(size_t GmlIdx, double h, int QalIdx, GmlxQuality *res)
+{
+   GETGMLPTR(gml, GmlIdx);
+   NatSct *n;
+   GmlDatSct *ver, *tet, *q = NULL;
+   GmlxQualStats st;
+
+   if(!ready(gml, &n, &ver, &tet))
+      return 0;
+   if(QalIdx)
+   {
+      if(QalIdx < 1 || QalIdx > GmlMaxDat || !gml->dat[QalIdx].use)
+         return 0;
+      q = &gml->dat[ QalIdx ];
+      if(q->ItmTyp != GmlFlt || q->NmbItm != 1 || q->NmbLin != n->nt)
+         return 0;
+   }
+   if(!n->NmbQalKrn)
+      n->NmbQalKrn = gml_new_kernel_slot(gml, GmlKrnGenerated + 100, "tet_quality");
+   gml_lib_timer_begin(gml, &gml->krn[ n->NmbQalKrn ]);
+   gmd_mesh_stats_init(gml->dev, n->stats, 1);
+   if(!gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, ver->GpuMem, det_threshold(h),
+                        q ? (float *)q->GpuMem : NULL, n->flags, n->stats))
+      return 0;
+   gml_lib_timer_end(gml, &gml->krn[ n->NmbQalKrn ]);
+   if(res)
+   {
+      if(!gmd_d2h(gml->dev, &st, n->stats, sizeof(st)))
+         return 0;
+      decode(&st, res);
+   }
+   return 1;
+}
+
+int GmlxInvertedFlags(size_t GmlIdx, unsigned *flags, size_t nwords)
+{
+   GETGMLPTR(gml, GmlIdx);
+   NatSct *n = gml->ext;
+   size_t need;
+   if(!n || !n->ready)
+      return 0;
+   need = (size_t)(n->nt + 31) / 32;
+   if(nwords < need)
+      return 0;
+   return gmd_d2h(gml->dev, flags, n->flags, need * sizeof(unsigned));
+}
+
+int GmlxSmoothQualityLoop(size_t GmlIdx, int nsweeps, float omega, double h, GmlxQuality *res)
+{
+   GETGMLPTR(gml, GmlIdx);
+   NatSct *n;
+   GmlDatSct *ver, *tet;
+   GmlxQualStats *st;
+
+   if(!ready(gml, &n, &ver, &tet) || nsweeps < 1 || nsweeps > n->nstats)
+      return 0;
+
+   if(!n->graph || n->gsweeps != nsweeps || n->gomega != omega || n->gh != h
+   || n->gver != ver->GpuMem || n->gtet != tet->GpuMem)
+   {
+      void *a = ver->GpuMem, *b = n->crd2;
+      gmd_graph_free(n->graph);
+      n->graph = NULL;
+      if(!gmd_graph_begin(gml->dev))
+         return 0;
+      gmd_mesh_stats_init(gml->dev, n->stats, nsweeps);
+      for(int s=0;s<nsweeps;s++)
+      {
+         gmd_mesh_laplace(gml->dev, n->nv, n->soff, n->pdeg, n->pcol, a, b, omega);
+         gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, b, det_threshold(h), NULL, n->flags,
+                          n->stats + s);
+         void *t = a; a = b; b = t;
+      }
+      if(a != ver->GpuMem)
+         gmd_d2d_async(gml->dev, ver->GpuMem, a, (size_t)n->nv * 16);
+      if(!gmd_graph_end(gml->dev, &n->graph))
+         return 0;
+      n->gsweeps = nsweeps;
+      n->gomega = omega;
+      n->gh = h;
+      n->gver = ver->GpuMem;
+      n->gtet = tet->GpuMem;
+   }
+
+   if(!n->NmbLoopKrn)
+      n->NmbLoopKrn = gml_new_kernel_slot(gml, GmlKrnGenerated + 100, "smooth_quality_graph");
+   gml_lib_timer_begin(gml, &gml->krn[ n->NmbLoopKrn ]);
+   if(!gmd_graph_launch(gml->dev, n->graph))
+      return 0;
+   gml_lib_timer_end(gml, &gml->krn[ n->NmbLoopKrn ]);
+
+   if(res)
+   {
+      st = malloc((size_t)nsweeps * sizeof(GmlxQualStats));
+      if(!st || !gmd_d2h(gml->dev, st, n->stats, (size_t)nsweeps * sizeof(GmlxQualStats)))
+      {
+         free(st);
+         return 0;
+      }
+      for(int s=0;s<nsweeps;s++)
+         decode(&st[s], &res[s]);
+      free(st);
+   }
+   return 1;
+}
+
+int GmlxMeshBytes(size_t GmlIdx, double *sweep_bytes, double *quality_bytes)
+{
+   GETGMLPTR(gml, GmlIdx);
+   NatSct *n = gml->ext;
+   if(!n || !n->ready)
+      return 0;
+   /* sweep: degree + used ball columns + own coordinates read + write;
+      quality: connectivity + coordinates once + flag words */
+   if(sweep_bytes)
+      *sweep_bytes = 4.0 * n->nv + 4.0 * (double)n->used + 32.0 * n->nv;
+   if(quality_bytes)
+      *quality_bytes = 16.0 * n->nt + 16.0 * n->nv + 4.0 * ((n->nt + 31) / 32);
+   return 1;
 }

@@ -66,6 +66,15 @@ int      GmlxSynchronize      (size_t);
 /* CUDA stream (cudaStream_t) that orders all work of the instance. */
 void    *GmlxStream           (size_t);
 
+/* CUDA events recorded on the instance stream, for timing device work from
+   foreign callers: create, record, elapsed seconds between two recorded
+   events (waits for the second), destroy.  No counterpart in the reference
+   (its per-kernel events are internal, gmlib3.c:3207-3208). */
+void    *GmlxEventCreate      (void);
+int      GmlxEventRecord      (size_t, void *evt);
+double   GmlxEventElapsed     (void *beg, void *end);
+void     GmlxEventDestroy     (void *evt);
+
 /* ---------------------------------------------------------------------------
  * Non-variadic forms for foreign-function interfaces
  * ------------------------------------------------------------------------- */
@@ -94,6 +103,70 @@ void    *GmlxDevicePtr        (size_t, int DatIdx);
  * ------------------------------------------------------------------------- */
 int      GmlxReduceArg        (size_t, int DatIdx, float *MinVal, int *MinIdx,
                                float *MaxVal, int *MaxIdx);
+
+/* ---------------------------------------------------------------------------
+ * Native tetrahedral mesh kernels: Laplacian smoothing over the ball of
+ * points and mean-ratio quality statistics.  They work on the instance's
+ * GmlVertices and GmlTetrahedra datatypes in place, without generated
+ * scatter/gather pairs.  No counterpart in the reference API (its
+ * NodeSmoothing example smooths through generated kernels,
+ * examples/NodeSmoothing/NodeSmoothing.c:128-171).
+ * ------------------------------------------------------------------------- */
+
+/* Device-side statistics of one quality pass (keys pack an order-preserving
+   image of the float quality in the high word and the tet index in the low
+   word; MaxKey stores the complemented image). */
+typedef struct
+{
+   unsigned long long MinKey, MaxKey;
+   double   Sum;
+   unsigned NmbInv, NmbF64;
+   unsigned Hist[64];
+}GmlxQualStats;
+
+/* Decoded statistics. */
+typedef struct
+{
+   float    MinQal, MaxQal;       /* signed mean-ratio quality */
+   int      MinIdx, MaxIdx;       /* smallest index on ties */
+   double   SumQal;               /* FP64 sum of the qualities */
+   unsigned NmbInv;              /* tets with det <= 0 (FP64 sign) */
+   unsigned NmbF64;              /* tets whose sign needed the FP64 determinant */
+   unsigned Hist[64];            /* bin = clamp(floor(64 q), 0, 63) */
+}GmlxQuality;
+
+/* Build the topology the native kernels need (vertex->tet lists and the
+   ball of points in SELL-32 form) on the GPU.  fix: 0 no vertex fixed,
+   1 vertices with a non-zero reference fixed, 2 vertices on the topological
+   boundary (faces owned by one tet) fixed.  Returns 1, or 0 on error (a ball
+   of more than 64 points). */
+int      GmlxMeshSetup        (size_t, int fix);
+
+/* Number of ball-of-points entries stored (sum of slice widths x 32) and
+   used (sum of degrees). */
+int      GmlxMeshBallInfo     (size_t, long long *stored, long long *used, int *maxdeg);
+
+/* nsweeps Jacobi sweeps x <- x + omega (mean of the ball of points - x) of
+   the vertex coordinates, in place; fixed vertices do not move. */
+int      GmlxSmooth           (size_t, int nsweeps, float omega);
+
+/* Mean-ratio quality q = 12 (3|V|)^(2/3) / sum of squared edge lengths of
+   every tet, negative when det <= 0; determinants whose FP32 magnitude is
+   below max(1e-6 h^3, the FP32 error bound) are recomputed in FP64.  QalIdx
+   (optional, 0 for none) receives q per tet (float tet solution).  The
+   inverted-element bit flags (bit t%32 of word t/32) are kept and returned
+   by GmlxInvertedFlags. */
+int      GmlxQualityStats     (size_t, double h, int QalIdx, GmlxQuality *res);
+int      GmlxInvertedFlags    (size_t, unsigned *flags, size_t nwords);
+
+/* The smoothing workload as one unit: nsweeps times (one sweep, then the
+   quality statistics), captured once as a CUDA graph and replayed; res
+   receives nsweeps results (may be NULL). */
+int      GmlxSmoothQualityLoop(size_t, int nsweeps, float omega, double h, GmlxQuality *res);
+
+/* Algorithmic (unique) bytes of one sweep and of one quality pass for the
+   current mesh, the numerators of the roofline figures. */
+int      GmlxMeshBytes        (size_t, double *sweep_bytes, double *quality_bytes);
 
 /* ---------------------------------------------------------------------------
  * Synthetic meshes and renumbering (host utilities).  No counterpart in the

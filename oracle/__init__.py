@@ -170,3 +170,48 @@ def ref_gather(crd, deg, ball, opt):
     res = np.zeros(len(crd), np.float32)
     r.ref_gather(_ptr(crd), len(crd), _ptr(deg), _ptr(ball), ball.shape[1], _ptr(opt), _ptr(res))
     return crd, res
+
+
+# ------------------------------------------------------ native mesh kernels
+
+def boundary_vertices(nv, tet):
+    tet = np.ascontiguousarray(tet, np.int32)
+    fixed = np.zeros(nv, np.int32)
+    lib().orc_boundary_vertices(nv, len(tet), _ptr(tet), _ptr(fixed))
+    return fixed
+
+
+def point_ball(nv, tet, fixed=None):
+    """CSR (ptr, col) of the distinct neighbours of each vertex, ascending;
+    fixed vertices get an empty ball."""
+    tet = np.ascontiguousarray(tet, np.int32)
+    fx = None if fixed is None else np.ascontiguousarray(fixed, np.int32)
+    f = lib().orc_point_ball
+    f.restype = ctypes.c_longlong
+    n = f(nv, len(tet), _ptr(tet), _ptr(fx), None, None, ctypes.c_longlong(0))
+    ptr = np.zeros(nv + 1, np.int64)
+    col = np.zeros(max(n, 1), np.int32)
+    f(nv, len(tet), _ptr(tet), _ptr(fx), _ptr(ptr), _ptr(col), ctypes.c_longlong(n))
+    return ptr, col[:n]
+
+
+def laplace(crd, ptr, col, omega, nsweeps):
+    c = np.array(crd, np.float64, copy=True)
+    lib().orc_laplace(len(c), _ptr(c), _ptr(np.ascontiguousarray(ptr, np.int64)),
+                      _ptr(np.ascontiguousarray(col, np.int32)), ctypes.c_double(omega), nsweeps)
+    return c
+
+
+def quality_stats(crd, tet):
+    """Mean-ratio q (FP64, signed by the FP64 determinant), 64-bin histogram,
+    inverted flags (bit words) and inverted count."""
+    crd = np.ascontiguousarray(crd, np.float32)
+    tet = np.ascontiguousarray(tet, np.int32)
+    nt = len(tet)
+    q = np.zeros(nt, np.float64)
+    hist = np.zeros(64, np.uint32)
+    flags = np.zeros((nt + 31) // 32, np.uint32)
+    ninv = ctypes.c_uint()
+    lib().orc_quality_stats(nt, _ptr(crd), _ptr(tet), _ptr(q), _ptr(hist), _ptr(flags),
+                            ctypes.byref(ninv))
+    return q, hist, flags, ninv.value

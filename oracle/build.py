@@ -34,11 +34,11 @@ def _run(cmd):
 
 
 def build_oracle(force=False):
-    srcs = [os.path.join(HERE, f) for f in ("oracle.c", "oracle_mesh.c", "oracle.h")]
+    names = ("oracle.c", "oracle_mesh.c", "baseline.c")
+    srcs = [os.path.join(HERE, f) for f in names + ("oracle.h",)]
     if force or _stale(LIB, srcs):
-        _run(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-std=gnu11",
-              os.path.join(HERE, "oracle.c"), os.path.join(HERE, "oracle_mesh.c"),
-              "-o", LIB, "-lm"])
+        _run(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-std=gnu11"]
+             + [os.path.join(HERE, f) for f in names] + ["-o", LIB, "-lm"])
     return LIB
 
 

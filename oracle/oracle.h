@@ -23,6 +23,14 @@ void   orc_scatter(int nt, const float *crd, const int *tet, double *opt);
 void   orc_gather(int nv, const float *crd, const int *deg, const int *ball, int width,
                   const double *opt, double *newcrd, double *res);
 
+/* oracle_mesh.c */
+long long orc_point_ball(int nv, int nt, const int *tet, const int *fixed,
+                         long long *ptr, int *col, long long cap);
+void   orc_boundary_vertices(int nv, int nt, const int *tet, int *fixed);
+void   orc_laplace(int nv, double *crd, const long long *ptr, const int *col, double w, int nsweeps);
+void   orc_quality_stats(int nt, const float *crd, const int *tet, double *q, unsigned *hist,
+                         unsigned *flags, unsigned *ninv);
+
 #ifdef __cplusplus
 }
 #endif

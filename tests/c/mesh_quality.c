@@ -91,7 +91,7 @@ int main(int argc, char **argv)
    for(i=0;i<nt;i++)
       GmlGetDataLine(GmlIdx, QalIdx, i, &q[i]);
 
-   printf("%.17g %.9g\n", sum, mn);
+   printf("%.17g %.17g\n", sum, mn);
 
    if(!(f = fopen(argv[3], "wb")))
       return 1;
