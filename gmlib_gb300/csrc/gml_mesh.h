@@ -18,15 +18,14 @@ int gmd_mesh_vt_csr(struct GmdCtx *ctx, const void *tet, int nt, int nv,
 int gmd_mesh_boundary(struct GmdCtx *ctx, const void *tet, int nt, const int *ptr,
                       const int *vt, int *fixed);
 int gmd_mesh_point_count(struct GmdCtx *ctx, const void *tet, int nv, const int *ptr,
-                         const int *vt, const int *fixed, int *pdeg,
-                         long long *width, long long *soff, int *err);
+                         const int *vt, const int *fixed, int *pdeg, int *pptr, int *err);
 int gmd_mesh_point_fill(struct GmdCtx *ctx, const void *tet, int nv, const int *ptr,
-                        const int *vt, const int *pdeg, const long long *soff, int *pcol);
-int gmd_mesh_laplace(struct GmdCtx *ctx, int nv, const long long *soff, const int *pdeg,
-                     const int *pcol, const void *in, void *out, float omega);
+                        const int *vt, const int *pptr, int *pcol);
+int gmd_mesh_laplace(struct GmdCtx *ctx, int nv, const int *pptr, const int *pcol,
+                     const void *in, void *out, float omega);
 int gmd_mesh_stats_init(struct GmdCtx *ctx, GmlxQualStats *st, int n);
 int gmd_mesh_quality(struct GmdCtx *ctx, int nt, const void *tet, const void *crd, float thr,
-                     float *qout, unsigned *flags, GmlxQualStats *st);
+                     float *qout, unsigned *flags, GmlxQualStats *st, int *err);
 
 /* CUDA graphs on the instance stream */
 int  gmd_graph_begin(struct GmdCtx *ctx);

@@ -8,21 +8,23 @@
  *                               fill (atomic slots; order within a ball is
  *                               not used by the kernels below)
  *   ball of points              per vertex, the distinct vertices of its
- *                               tetrahedra, sorted ascending, stored in
- *                               SELL-32 (slices of 32 vertices, column-major,
- *                               slice width = longest ball in the slice);
- *                               fixed vertices get an empty ball
+ *                               tetrahedra, sorted ascending, in CSR form;
+ *                               each entry carries the row of its vertex
+ *                               inside the vertex's group of 32; fixed
+ *                               vertices get an empty ball
  *   boundary vertices           vertices of faces owned by a single tet
  *
  * Hot kernels (HBM-bound):
- *   laplace_sell   one Jacobi sweep x' = x + w (mean(ball) - x); per vertex
- *                  4 (degree) + 4 deg (columns, 128-byte runs per warp)
- *                  + 16 (own) + 16 (write) bytes; the neighbour gathers hit
- *                  L2 (coordinates are 16 V bytes).
+ *   laplace_warp   one Jacobi sweep x' = x + w (mean(ball) - x), one warp
+ *                  per 32 consecutive vertices; per vertex 4 (row pointer)
+ *                  + 4 deg (entries, streamed in 128-byte runs) + 16 (own)
+ *                  + 16 (write) bytes; neighbour gathers hit L2 (the
+ *                  coordinates are 16 V bytes).
  *   tet_quality    mean-ratio quality 12 (3|V|)^(2/3) / sum l^2 signed by
  *                  orientation, 64-bin histogram, min/argmin, max/argmax,
- *                  sum, inverted-element count and bit flags; 16 bytes of
- *                  connectivity per tet streamed, coordinates from L2.  The
+ *                  sum, inverted-element count and bit flags; the 16 bytes
+ *                  per tet of connectivity are staged through shared memory
+ *                  by TMA bulk copies, coordinates come from L2.  The
  *                  determinant is recomputed in FP64 whenever the FP32 value
  *                  is below max(1e-6 h^3, 16 eps32 * permanent), a bound on
  *                  the FP32 error, so the orientation flags are exact.
@@ -151,10 +153,12 @@ __global__ void boundary_kernel(const int4 *__restrict__ tet, int nt, const int 
 }
 
 /* ========================================================================= */
-/* ball of points                                                             */
+/* ball of points (CSR, entries tagged with the row inside its warp group)    */
 /* ========================================================================= */
 
 #define PB_MAX 64
+#define PB_ROW_SHIFT 27
+#define PB_COL_MASK ((1 << PB_ROW_SHIFT) - 1)
 
 /* distinct vertices of the tets around v, ascending; returns the count or
    -1 when the ball exceeds PB_MAX */
@@ -199,59 +203,102 @@ __global__ void point_count_kernel(int nv, const int4 *__restrict__ tet, const i
    pdeg[v] = n;
 }
 
-__global__ void slice_width_kernel(int nv, const int *__restrict__ pdeg, long long *w)
-{
-   int s = blockIdx.x * blockDim.x + threadIdx.x, ns = (nv + 31) / 32;
-   if(s >= ns) return;
-   int m = 0;
-   for(int r=s*32;r<s*32+32 && r<nv;r++)
-      m = max(m, pdeg[r]);
-   w[s] = m;
-}
-
+/* entry = (v & 31) << 27 | neighbour: the row of v inside its group of 32
+   vertices travels with the column so that a warp can reduce a group's
+   contiguous entries without a search */
 __global__ void point_fill_kernel(int nv, const int4 *__restrict__ tet, const int *__restrict__ ptr,
-                                  const int *__restrict__ vt, const int *__restrict__ pdeg,
-                                  const long long *__restrict__ soff, int *pcol)
+                                  const int *__restrict__ vt, const int *__restrict__ pptr,
+                                  int *pcol)
 {
    int v = blockIdx.x * blockDim.x + threadIdx.x;
    int lst[PB_MAX];
-   if(v >= nv || pdeg[v] == 0) return;
+   if(v >= nv) return;
+   int d = pptr[v+1] - pptr[v];
+   if(!d) return;
    int n = point_ball(v, tet, ptr, vt, lst);
-   long long base = soff[v >> 5];
-   for(int k=0;k<n && k<pdeg[v];k++)
-      pcol[ (base + k) * 32 + (v & 31) ] = lst[k];
+   for(int k=0;k<n && k<d;k++)
+      pcol[ pptr[v] + k ] = ((v & 31) << PB_ROW_SHIFT) | lst[k];
 }
 
 /* ========================================================================= */
-/* Laplacian sweep over the ball of points                                    */
+/* Laplacian sweep: one warp per group of 32 consecutive vertices             */
 /* ========================================================================= */
 
+/* The group's entries are contiguous in the CSR arrays; the warp streams
+   them 32 at a time (coalesced 128-byte column loads, 32 independent
+   coordinate gathers), sums each row's run with a shuffle segmented scan
+   whose tail lane adds into shared memory (one writer per row and chunk,
+   chunks in order: the summation order is fixed, results are
+   reproducible), then lane r updates vertex 32g + r. */
 __global__ void __launch_bounds__(MK_THREADS)
-laplace_sell_kernel(int nv, const long long *__restrict__ soff, const int *__restrict__ pdeg,
-                    const int *__restrict__ pcol, const float4 *__restrict__ in,
-                    float4 *__restrict__ out, float omega)
+laplace_warp_kernel(int nv, const int *__restrict__ pptr, const int *__restrict__ pcol,
+                    const float4 *__restrict__ in, float4 *__restrict__ out, float omega)
 {
-   int v = blockIdx.x * blockDim.x + threadIdx.x;
-   if(v >= nv) return;
-   const int d = __ldg(&pdeg[v]);
-   const float4 p = __ldg(&in[v]);
-   if(d == 0)
-   {
-      out[v] = p;
+   __shared__ float acc[MK_THREADS / 32][3][32];
+   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+   const int v0 = (blockIdx.x * MK_THREADS + threadIdx.x) & ~31;
+   if(v0 >= nv)
       return;
-   }
-   const int *cp = pcol + __ldg(&soff[v >> 5]) * 32 + (v & 31);
-   float sx = 0.f, sy = 0.f, sz = 0.f;
-#pragma unroll 4
-   for(int k=0;k<d;k++)
+   const int v = v0 + lane;
+   const int vl = v < nv ? v : nv;
+   const int e0 = __ldg(&pptr[v0]);
+   const int p0 = __ldg(&pptr[vl]), p1 = __ldg(&pptr[v < nv ? v + 1 : nv]);
+   const int e1 = __shfl_sync(0xffffffffu, p1, 31);
+   float *ax = acc[wid][0], *ay = acc[wid][1], *az = acc[wid][2];
+
+   ax[lane] = 0.f; ay[lane] = 0.f; az[lane] = 0.f;
+   __syncwarp();
+
+   for(int base=e0; base<e1; base+=64)
    {
-      const int c = __ldg(cp + (size_t)k * 32);
-      const float4 q = __ldg(&in[c]);
-      sx += q.x; sy += q.y; sz += q.z;
+      /* two chunks of 32 entries in flight */
+      const int ea = base + lane, eb = base + 32 + lane;
+      const int ka = ea < e1 ? __ldg(&pcol[ea]) : -1;
+      const int kb = eb < e1 ? __ldg(&pcol[eb]) : -1;
+      float4 qa = make_float4(0.f, 0.f, 0.f, 0.f), qb = qa;
+      if(ka >= 0) qa = __ldg(&in[ ka & PB_COL_MASK ]);
+      if(kb >= 0) qb = __ldg(&in[ kb & PB_COL_MASK ]);
+#pragma unroll
+      for(int h=0;h<2;h++)
+      {
+         const int key = h ? kb : ka;
+         const int r = key >= 0 ? (key >> PB_ROW_SHIFT) : -1;
+         float x = h ? qb.x : qa.x, y = h ? qb.y : qa.y, z = h ? qb.z : qa.z;
+#pragma unroll
+         for(int o=1;o<32;o<<=1)
+         {
+            const float xo = __shfl_up_sync(0xffffffffu, x, o);
+            const float yo = __shfl_up_sync(0xffffffffu, y, o);
+            const float zo = __shfl_up_sync(0xffffffffu, z, o);
+            const int ro = __shfl_up_sync(0xffffffffu, r, o);
+            if(lane >= o && ro == r)
+            {
+               x += xo; y += yo; z += zo;
+            }
+         }
+         const int rn = __shfl_down_sync(0xffffffffu, r, 1);
+         if(r >= 0 && (lane == 31 || rn != r))
+         {
+            ax[r] += x; ay[r] += y; az[r] += z;
+         }
+         __syncwarp();
+      }
    }
-   const float inv = 1.0f / (float)d;
-   out[v] = make_float4(p.x + omega * (sx * inv - p.x), p.y + omega * (sy * inv - p.y),
-                        p.z + omega * (sz * inv - p.z), 0.f);
+
+   if(v < nv)
+   {
+      const float4 p = __ldg(&in[v]);
+      const int d = p1 - p0;
+      if(d == 0)
+         out[v] = p;
+      else
+      {
+         const float inv = 1.0f / (float)d;
+         out[v] = make_float4(p.x + omega * (ax[lane] * inv - p.x),
+                              p.y + omega * (ay[lane] * inv - p.y),
+                              p.z + omega * (az[lane] * inv - p.z), 0.f);
+      }
+   }
 }
 
 /* ========================================================================= */
@@ -278,93 +325,82 @@ __global__ void stats_init_kernel(GmlxQualStats *st, int n)
       s->Hist[b] = 0;
 }
 
-__global__ void __launch_bounds__(MK_THREADS)
-tet_quality_kernel(int nt, const int4 *__restrict__ tet, const float4 *__restrict__ crd,
-                   float thr, float *__restrict__ qout, unsigned *__restrict__ flags,
-                   GmlxQualStats *st)
+/* signed mean-ratio quality of one tet; *inv = det <= 0 (FP64 sign when the
+   FP32 determinant is below the threshold or its error bound), *f64 = 1
+   when the FP64 determinant was used */
+__device__ __forceinline__ float tet_mean_ratio(const int4 e, const float4 *__restrict__ crd,
+                                                float thr, int *inv, int *f64)
 {
-   __shared__ unsigned hist[64];
+   const float4 a = __ldg(&crd[e.x]), b = __ldg(&crd[e.y]);
+   const float4 c = __ldg(&crd[e.z]), d = __ldg(&crd[e.w]);
+   const float abx = b.x - a.x, aby = b.y - a.y, abz = b.z - a.z;
+   const float acx = c.x - a.x, acy = c.y - a.y, acz = c.z - a.z;
+   const float adx = d.x - a.x, ady = d.y - a.y, adz = d.z - a.z;
+   const float m1 = acy * adz - acz * ady, m2 = acz * adx - acx * adz, m3 = acx * ady - acy * adx;
+   float det = abx * m1 + aby * m2 + abz * m3;
+   int pos = det > 0.f;
+   const float perm = fabsf(abx) * (fabsf(acy * adz) + fabsf(acz * ady))
+                    + fabsf(aby) * (fabsf(acz * adx) + fabsf(acx * adz))
+                    + fabsf(abz) * (fabsf(acx * ady) + fabsf(acy * adx));
+   *f64 = 0;
+   if(fabsf(det) < fmaxf(thr, 9.5367431640625e-07f * perm))
+   {
+      const double Ax = a.x, Ay = a.y, Az = a.z;
+      const double bx = b.x - Ax, by = b.y - Ay, bz = b.z - Az;
+      const double cx = c.x - Ax, cy = c.y - Ay, cz = c.z - Az;
+      const double dx = d.x - Ax, dy = d.y - Ay, dz = d.z - Az;
+      const double dd = bx * (cy * dz - cz * dy) + by * (cz * dx - cx * dz) + bz * (cx * dy - cy * dx);
+      det = (float)dd;
+      pos = dd > 0.;
+      *f64 = 1;
+   }
+   const float bcx = c.x - b.x, bcy = c.y - b.y, bcz = c.z - b.z;
+   const float bdx = d.x - b.x, bdy = d.y - b.y, bdz = d.z - b.z;
+   const float cdx = d.x - c.x, cdy = d.y - c.y, cdz = d.z - c.z;
+   const float l2 = abx*abx + aby*aby + abz*abz + acx*acx + acy*acy + acz*acz
+                  + adx*adx + ady*ady + adz*adz + bcx*bcx + bcy*bcy + bcz*bcz
+                  + bdx*bdx + bdy*bdy + bdz*bdz + cdx*cdx + cdy*cdy + cdz*cdz;
+   const float cb = cbrtf(0.5f * fabsf(det));          /* (3 |det| / 6)^(1/3) */
+   const float q = 12.0f * cb * cb / l2;
+   *inv = !pos;
+   return pos ? q : -q;
+}
+
+/* per-thread accumulators of the statistics */
+struct QAcc
+{
+   unsigned long long kmin, kmax;
+   float s, c;
+   unsigned ninv, nf64;
+};
+
+__device__ __forceinline__ void qacc_add(QAcc &a, float q, int t, int f64, unsigned *hist)
+{
+   int bin = (int)(q * 64.0f);
+   bin = bin < 0 ? 0 : (bin > 63 ? 63 : bin);
+   atomicAdd(&hist[bin], 1u);
+   const unsigned k = mk_fkey(q);
+   const unsigned long long a64 = ((unsigned long long)k << 32) | (unsigned)t;
+   const unsigned long long b64 = ((unsigned long long)(~k) << 32) | (unsigned)t;
+   a.kmin = a64 < a.kmin ? a64 : a.kmin;
+   a.kmax = b64 < a.kmax ? b64 : a.kmax;
+   const float tt = a.s + q, bp = tt - a.s;
+   a.c += (a.s - (tt - bp)) + (q - bp);
+   a.s = tt;
+   a.nf64 += f64;
+}
+
+/* block reduction of the accumulators into the global statistics */
+__device__ __forceinline__ void qacc_flush(QAcc &a, unsigned *hist, GmlxQualStats *st)
+{
    __shared__ unsigned long long smin[MK_THREADS / 32], smax[MK_THREADS / 32];
    __shared__ double ssum[MK_THREADS / 32];
    __shared__ unsigned sinv[MK_THREADS / 32], sf64[MK_THREADS / 32];
-
    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-   unsigned long long kmin = ~0ULL, kmax = ~0ULL;
-   float s = 0.f, c = 0.f;
-   unsigned ninv = 0, nf64 = 0;
+   double dsum = (double)a.s + (double)a.c;
+   unsigned long long kmin = a.kmin, kmax = a.kmax;
+   unsigned ninv = a.ninv, nf64 = a.nf64;
 
-   if(threadIdx.x < 64)
-      hist[threadIdx.x] = 0;
-   __syncthreads();
-
-   const int stride = gridDim.x * blockDim.x;
-   /* every warp handles 32 consecutive tets per iteration (ballot words) */
-   for(int base=blockIdx.x*blockDim.x + wid*32; base<nt; base+=stride)
-   {
-      const int t = base + lane;
-      int inv = 0;
-      if(t < nt)
-      {
-         const int4 e = __ldg(&tet[t]);
-         const float4 a = __ldg(&crd[e.x]), b = __ldg(&crd[e.y]);
-         const float4 cc = __ldg(&crd[e.z]), d = __ldg(&crd[e.w]);
-         const float abx = b.x - a.x, aby = b.y - a.y, abz = b.z - a.z;
-         const float acx = cc.x - a.x, acy = cc.y - a.y, acz = cc.z - a.z;
-         const float adx = d.x - a.x, ady = d.y - a.y, adz = d.z - a.z;
-         const float bcx = cc.x - b.x, bcy = cc.y - b.y, bcz = cc.z - b.z;
-         const float bdx = d.x - b.x, bdy = d.y - b.y, bdz = d.z - b.z;
-         const float cdx = d.x - cc.x, cdy = d.y - cc.y, cdz = d.z - cc.z;
-         const float m1 = acy * adz - acz * ady, m2 = acz * adx - acx * adz, m3 = acx * ady - acy * adx;
-         float det = abx * m1 + aby * m2 + abz * m3;
-         int pos = det > 0.f;
-         const float perm = fabsf(abx) * (fabsf(acy * adz) + fabsf(acz * ady))
-                          + fabsf(aby) * (fabsf(acz * adx) + fabsf(acx * adz))
-                          + fabsf(abz) * (fabsf(acx * ady) + fabsf(acy * adx));
-         if(fabsf(det) < fmaxf(thr, 9.5367431640625e-07f * perm))
-         {
-            /* FP64 determinant of the FP32 coordinates decides the sign */
-            const double Ax = a.x, Ay = a.y, Az = a.z;
-            const double bx = b.x - Ax, by = b.y - Ay, bz = b.z - Az;
-            const double cx = cc.x - Ax, cy = cc.y - Ay, cz = cc.z - Az;
-            const double dx = d.x - Ax, dy = d.y - Ay, dz = d.z - Az;
-            const double dd = bx * (cy * dz - cz * dy) + by * (cz * dx - cx * dz) + bz * (cx * dy - cy * dx);
-            det = (float)dd;
-            pos = dd > 0.;
-            nf64++;
-         }
-         const float l2 = abx*abx + aby*aby + abz*abz + acx*acx + acy*acy + acz*acz
-                        + adx*adx + ady*ady + adz*adz + bcx*bcx + bcy*bcy + bcz*bcz
-                        + bdx*bdx + bdy*bdy + bdz*bdz + cdx*cdx + cdy*cdy + cdz*cdz;
-         const float vol = fabsf(det) * (1.0f / 6.0f);
-         const float cb = cbrtf(3.0f * vol);
-         float q = 12.0f * cb * cb / l2;
-         inv = !pos;
-         if(inv) q = -q;
-         if(qout) qout[t] = q;
-         int bin = (int)(q * 64.0f);
-         bin = bin < 0 ? 0 : (bin > 63 ? 63 : bin);
-         atomicAdd(&hist[bin], 1u);
-         const unsigned k = mk_fkey(q);
-         const unsigned long long a64 = ((unsigned long long)k << 32) | (unsigned)t;
-         const unsigned long long b64 = ((unsigned long long)(~k) << 32) | (unsigned)t;
-         kmin = a64 < kmin ? a64 : kmin;
-         kmax = b64 < kmax ? b64 : kmax;
-         /* TwoSum accumulation */
-         const float tt = s + q, bp = tt - s;
-         c += (s - (tt - bp)) + (q - bp);
-         s = tt;
-      }
-      const unsigned word = __ballot_sync(0xffffffffu, inv);
-      if(lane == 0)
-      {
-         ninv += __popc(word);
-         if(flags)
-            flags[ base >> 5 ] = word;
-      }
-   }
-
-   /* block reduction */
-   double dsum = (double)s + (double)c;
    for(int o=16;o>0;o>>=1)
    {
       unsigned long long x = __shfl_xor_sync(0xffffffffu, kmin, o);
@@ -373,6 +409,7 @@ tet_quality_kernel(int nt, const int4 *__restrict__ tet, const float4 *__restric
       kmax = y < kmax ? y : kmax;
       dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
       nf64 += __shfl_xor_sync(0xffffffffu, nf64, o);
+      ninv += __shfl_xor_sync(0xffffffffu, ninv, o);
    }
    if(lane == 0)
    {
@@ -397,6 +434,163 @@ tet_quality_kernel(int nt, const int4 *__restrict__ tet, const float4 *__restric
    }
    if(threadIdx.x < 64 && hist[threadIdx.x])
       atomicAdd(&st->Hist[threadIdx.x], hist[threadIdx.x]);
+}
+
+/* ------------------------------------------------------------------------- */
+/* TMA bulk copies and mbarriers (inline PTX)                                 */
+/* ------------------------------------------------------------------------- */
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+   return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                             unsigned long long *bar)
+{
+   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ int mbar_try_wait(unsigned long long *bar, unsigned parity)
+{
+   unsigned ok;
+   asm volatile("{\n\t.reg .pred p;\n\t"
+                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+   return (int)ok;
+}
+
+/* bounded wait: gives up after QK_SPIN polls (each try_wait may itself
+   suspend for a while), so a lost transfer ends the kernel instead of
+   hanging it */
+#define QK_SPIN (1 << 20)
+
+__device__ __forceinline__ int mbar_wait_bounded(unsigned long long *bar, unsigned parity)
+{
+   for(int i=0;i<QK_SPIN;i++)
+      if(mbar_try_wait(bar, parity))
+         return 1;
+   return 0;
+}
+
+#define QK_CHUNK  1024                     /* tets per stage: 16 KB */
+#define QK_STAGES 3
+#define QK_SMEM   (QK_STAGES * QK_CHUNK * 16)
+
+/* The tetrahedron stream (16 bytes per tet, read once) is staged through
+   shared memory by TMA bulk copies, QK_STAGES chunks ahead; the coordinate
+   gathers (16 V bytes, L2 resident) are issued from registers, two tets per
+   thread at a time.  Each warp handles 32 consecutive tets per pass, so its
+   ballot is one word of the inverted-element bit flags. */
+__global__ void __launch_bounds__(MK_THREADS, 4)
+tet_quality_tma_kernel(int nt, const int4 *__restrict__ tet, const float4 *__restrict__ crd,
+                       float thr, float *__restrict__ qout, unsigned *__restrict__ flags,
+                       GmlxQualStats *st, int *err)
+{
+   extern __shared__ __align__(128) unsigned char qk_smem[];
+   __shared__ __align__(8) unsigned long long bar[QK_STAGES];
+   __shared__ unsigned hist[64];
+   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+   const int nchunk = (nt + QK_CHUNK - 1) / QK_CHUNK;
+   const int mine = blockIdx.x < nchunk ? (nchunk - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+   int4 *stage = (int4 *)qk_smem;
+   QAcc a = { ~0ULL, ~0ULL, 0.f, 0.f, 0u, 0u };
+
+   if(threadIdx.x < 64)
+      hist[threadIdx.x] = 0;
+   if(threadIdx.x == 0)
+   {
+      for(int s=0;s<QK_STAGES;s++)
+         mbar_init(&bar[s], 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      for(int s=0;s<QK_STAGES && s<mine;s++)
+      {
+         const int start = (blockIdx.x + s * gridDim.x) * QK_CHUNK;
+         const unsigned bytes = (unsigned)(min(QK_CHUNK, nt - start) * 16);
+         mbar_expect_tx(&bar[s], bytes);
+         tma_bulk_g2s(stage + s * QK_CHUNK, tet + start, bytes, &bar[s]);
+      }
+   }
+   __syncthreads();
+
+   for(int i=0;i<mine;i++)
+   {
+      const int s = i % QK_STAGES;
+      const unsigned parity = (unsigned)((i / QK_STAGES) & 1);
+      const int ok = mbar_wait_bounded(&bar[s], parity);
+      if(__syncthreads_or(!ok))
+      {
+         /* lost transfer: report, let the issued copies land, stop */
+         if(threadIdx.x == 0)
+         {
+            atomicOr(err, 4);
+            for(int j=i;j<mine && j<i+QK_STAGES;j++)
+               mbar_wait_bounded(&bar[j % QK_STAGES], (unsigned)((j / QK_STAGES) & 1));
+         }
+         __syncthreads();
+         return;
+      }
+
+      const int start = (blockIdx.x + i * gridDim.x) * QK_CHUNK;
+      const int n = min(QK_CHUNK, nt - start);
+      const int4 *chunk = stage + s * QK_CHUNK;
+
+      /* 4 passes of 256 tets; a thread takes tets j and j + 512 together */
+#pragma unroll 1
+      for(int pass=0;pass<2;pass++)
+      {
+         const int j0 = pass * 2 * MK_THREADS + wid * 32 + lane;
+         const int j1 = j0 + MK_THREADS;
+         int inv0 = 0, inv1 = 0, f0 = 0, f1 = 0;
+         float q0 = 0.f, q1 = 0.f;
+         if(j0 < n) q0 = tet_mean_ratio(chunk[j0], crd, thr, &inv0, &f0);
+         if(j1 < n) q1 = tet_mean_ratio(chunk[j1], crd, thr, &inv1, &f1);
+         if(j0 < n)
+         {
+            qacc_add(a, q0, start + j0, f0, hist);
+            if(qout) qout[start + j0] = q0;
+         }
+         if(j1 < n)
+         {
+            qacc_add(a, q1, start + j1, f1, hist);
+            if(qout) qout[start + j1] = q1;
+         }
+         const unsigned w0 = __ballot_sync(0xffffffffu, inv0);
+         const unsigned w1 = __ballot_sync(0xffffffffu, inv1);
+         if(lane == 0)
+         {
+            const int b0 = pass * 2 * MK_THREADS + wid * 32, b1 = b0 + MK_THREADS;
+            a.ninv += __popc(w0) + __popc(w1);
+            if(flags && b0 < n) flags[ (start + b0) >> 5 ] = w0;
+            if(flags && b1 < n) flags[ (start + b1) >> 5 ] = w1;
+         }
+      }
+
+      /* every thread is done with stage s: refill it */
+      __syncthreads();
+      if(threadIdx.x == 0 && i + QK_STAGES < mine)
+      {
+         const int nstart = (blockIdx.x + (i + QK_STAGES) * gridDim.x) * QK_CHUNK;
+         const unsigned bytes = (unsigned)(min(QK_CHUNK, nt - nstart) * 16);
+         mbar_expect_tx(&bar[s], bytes);
+         tma_bulk_g2s(stage + s * QK_CHUNK, tet + nstart, bytes, &bar[s]);
+      }
+   }
+
+   qacc_flush(a, hist, st);
 }
 
 /* ========================================================================= */
@@ -426,30 +620,28 @@ extern "C" int gmd_mesh_boundary(GmdCtx *ctx, const void *tet, int nt, const int
 }
 
 extern "C" int gmd_mesh_point_count(GmdCtx *ctx, const void *tet, int nv, const int *ptr,
-                                    const int *vt, const int *fixed, int *pdeg,
-                                    long long *width, long long *soff, int *err)
+                                    const int *vt, const int *fixed, int *pdeg, int *pptr,
+                                    int *err)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
-   int ns = (nv + 31) / 32;
    point_count_kernel<<<nblk(nv, 128), 128, 0, st>>>(nv, (const int4 *)tet, ptr, vt, fixed, pdeg, err);
-   slice_width_kernel<<<nblk(ns, MK_THREADS), MK_THREADS, 0, st>>>(nv, pdeg, width);
-   scan_excl_kernel<long long><<<1, 1024, 0, st>>>(width, soff, ns);
+   scan_excl_kernel<int><<<1, 1024, 0, st>>>(pdeg, pptr, nv);
    return cudaGetLastError() == cudaSuccess;
 }
 
 extern "C" int gmd_mesh_point_fill(GmdCtx *ctx, const void *tet, int nv, const int *ptr,
-                                   const int *vt, const int *pdeg, const long long *soff, int *pcol)
+                                   const int *vt, const int *pptr, int *pcol)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
-   point_fill_kernel<<<nblk(nv, 128), 128, 0, st>>>(nv, (const int4 *)tet, ptr, vt, pdeg, soff, pcol);
+   point_fill_kernel<<<nblk(nv, 128), 128, 0, st>>>(nv, (const int4 *)tet, ptr, vt, pptr, pcol);
    return cudaGetLastError() == cudaSuccess;
 }
 
-extern "C" int gmd_mesh_laplace(GmdCtx *ctx, int nv, const long long *soff, const int *pdeg,
-                                const int *pcol, const void *in, void *out, float omega)
+extern "C" int gmd_mesh_laplace(GmdCtx *ctx, int nv, const int *pptr, const int *pcol,
+                                const void *in, void *out, float omega)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
-   laplace_sell_kernel<<<nblk(nv, MK_THREADS), MK_THREADS, 0, st>>>(nv, soff, pdeg, pcol,
+   laplace_warp_kernel<<<nblk(nv, MK_THREADS), MK_THREADS, 0, st>>>(nv, pptr, pcol,
       (const float4 *)in, (float4 *)out, omega);
    return cudaGetLastError() == cudaSuccess;
 }
@@ -462,14 +654,23 @@ extern "C" int gmd_mesh_stats_init(GmdCtx *ctx, GmlxQualStats *st, int n)
 }
 
 extern "C" int gmd_mesh_quality(GmdCtx *ctx, int nt, const void *tet, const void *crd, float thr,
-                                float *qout, unsigned *flags, GmlxQualStats *st)
+                                float *qout, unsigned *flags, GmlxQualStats *st, int *err)
 {
+   static int attr_set = 0;
    cudaStream_t s = (cudaStream_t)gmd_stream(ctx);
-   long long need = nblk(nt, MK_THREADS);
-   long long cap = (long long)gmd_num_sms(ctx) * 8;
+   long long need = nblk(nt, QK_CHUNK);
+   long long cap = (long long)gmd_num_sms(ctx) * 4;
    unsigned g = (unsigned)(need < cap ? need : cap);
-   if(g < 1) g = 1;
-   tet_quality_kernel<<<g, MK_THREADS, 0, s>>>(nt, (const int4 *)tet, (const float4 *)crd, thr,
-                                               qout, flags, st);
+   if(nt <= 0)
+      return 1;
+   if(!attr_set)
+   {
+      if(cudaFuncSetAttribute(tet_quality_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              QK_SMEM) != cudaSuccess)
+         return 0;
+      attr_set = 1;
+   }
+   tet_quality_tma_kernel<<<g, MK_THREADS, QK_SMEM, s>>>(nt, (const int4 *)tet, (const float4 *)crd,
+                                                         thr, qout, flags, st, err);
    return cudaGetLastError() == cudaSuccess;
 }

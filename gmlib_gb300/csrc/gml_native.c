@@ -14,9 +14,8 @@
 typedef struct
 {
    int         nv, nt, fix, ready;
-   int         *ptr, *vt, *tmp, *err, *fixed, *pdeg, *pcol;
-   long long   *width, *soff;
-   long long   ncol, used;
+   int         *ptr, *vt, *tmp, *err, *fixed, *pdeg, *pptr, *pcol;
+   long long   used;
    int         maxdeg;
    void        *crd2;                 /* second coordinate buffer */
    unsigned    *flags;                /* inverted-element bits */
@@ -45,8 +44,8 @@ static void free_state(GmlSct *gml, NatSct *n)
    gmd_free(gml->dev, n->ptr);   gmd_free(gml->dev, n->vt);
    gmd_free(gml->dev, n->tmp);   gmd_free(gml->dev, n->err);
    gmd_free(gml->dev, n->fixed); gmd_free(gml->dev, n->pdeg);
-   gmd_free(gml->dev, n->pcol);  gmd_free(gml->dev, n->width);
-   gmd_free(gml->dev, n->soff);  gmd_free(gml->dev, n->crd2);
+   gmd_free(gml->dev, n->pcol);  gmd_free(gml->dev, n->pptr);
+   gmd_free(gml->dev, n->crd2);
    gmd_free(gml->dev, n->flags); gmd_free(gml->dev, n->stats);
    gmd_graph_free(n->graph);
    memset(n, 0, sizeof(NatSct));
@@ -79,8 +78,7 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
    GETGMLPTR(gml, GmlIdx);
    GmlDatSct *ver, *tet;
    NatSct *n;
-   int nv, nt, err = 0, ns, *pdeg_h;
-   long long *soff_h;
+   int nv, nt, err = 0, *pdeg_h, tot;
 
    if(gml->Offline || !mesh_dat(gml, &ver, &tet))
       return 0;
@@ -89,7 +87,11 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
    free_state(gml, n);
    nv = ver->NmbLin;
    nt = tet->NmbLin;
-   ns = (nv + 31) / 32;
+   if(nv >= (1 << 27))
+   {
+      puts("GmlxMeshSetup: more than 2^27 vertices");
+      return 0;
+   }
    n->nv = nv;
    n->nt = nt;
    n->fix = fix;
@@ -99,13 +101,12 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
    n->tmp   = gmd_alloc(gml->dev, (size_t)nv * sizeof(int));
    n->err   = gmd_alloc(gml->dev, sizeof(int));
    n->pdeg  = gmd_alloc(gml->dev, (size_t)nv * sizeof(int));
-   n->width = gmd_alloc(gml->dev, (size_t)(ns + 1) * sizeof(long long));
-   n->soff  = gmd_alloc(gml->dev, (size_t)(ns + 1) * sizeof(long long));
+   n->pptr  = gmd_alloc(gml->dev, (size_t)(nv + 1) * sizeof(int));
    n->crd2  = gmd_alloc(gml->dev, (size_t)nv * 16);
    n->flags = gmd_alloc(gml->dev, (size_t)((nt + 31) / 32) * sizeof(unsigned));
    n->stats = gmd_alloc(gml->dev, GML_MAXSTATS * sizeof(GmlxQualStats));
    n->nstats = GML_MAXSTATS;
-   if(!n->ptr || !n->vt || !n->tmp || !n->err || !n->pdeg || !n->width || !n->soff
+   if(!n->ptr || !n->vt || !n->tmp || !n->err || !n->pdeg || !n->pptr
    || !n->crd2 || !n->flags || !n->stats)
    {
       free_state(gml, n);
@@ -139,47 +140,40 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
    }
 
    gmd_mesh_point_count(gml->dev, tet->GpuMem, nv, n->ptr, n->vt, n->fixed, n->pdeg,
-                        n->width, n->soff, n->err);
+                        n->pptr, n->err);
 
-   soff_h = malloc((size_t)(ns + 1) * sizeof(long long));
    pdeg_h = malloc((size_t)nv * sizeof(int));
-   if(!soff_h || !pdeg_h)
+   if(!pdeg_h)
    {
-      free(soff_h); free(pdeg_h);
       free_state(gml, n);
       return 0;
    }
    gmd_d2h(gml->dev, &err, n->err, sizeof(int));
-   gmd_d2h(gml->dev, soff_h, n->soff, (size_t)(ns + 1) * sizeof(long long));
+   gmd_d2h(gml->dev, &tot, n->pptr + nv, sizeof(int));
    gmd_d2h(gml->dev, pdeg_h, n->pdeg, (size_t)nv * sizeof(int));
 
    if(err)
    {
       printf("GmlxMeshSetup: %s\n", (err & 2) ? "vertex index out of range in the tetrahedra"
                                                : "a ball of points exceeds 64 vertices");
-      free(soff_h); free(pdeg_h);
+      free(pdeg_h);
       free_state(gml, n);
       return 0;
    }
 
-   n->ncol = soff_h[ns];
-   n->used = 0;
+   n->used = tot;
    n->maxdeg = 0;
    for(int i=0;i<nv;i++)
-   {
-      n->used += pdeg_h[i];
       if(pdeg_h[i] > n->maxdeg) n->maxdeg = pdeg_h[i];
-   }
-   free(soff_h);
    free(pdeg_h);
 
-   n->pcol = gmd_alloc(gml->dev, (size_t)(n->ncol > 0 ? n->ncol : 1) * 32 * sizeof(int));
+   n->pcol = gmd_alloc(gml->dev, (size_t)(tot > 0 ? tot : 1) * sizeof(int));
    if(!n->pcol)
    {
       free_state(gml, n);
       return 0;
    }
-   gmd_mesh_point_fill(gml->dev, tet->GpuMem, nv, n->ptr, n->vt, n->pdeg, n->soff, n->pcol);
+   gmd_mesh_point_fill(gml->dev, tet->GpuMem, nv, n->ptr, n->vt, n->pptr, n->pcol);
    gmd_sync(gml->dev);
    n->ready = 1;
    return 1;
@@ -191,7 +185,7 @@ int GmlxMeshBallInfo(size_t GmlIdx, long long *stored, long long *used, int *max
    NatSct *n = gml->ext;
    if(!n || !n->ready)
       return 0;
-   if(stored) *stored = n->ncol * 32;
+   if(stored) *stored = n->used;
    if(used) *used = n->used;
    if(maxdeg) *maxdeg = n->maxdeg;
    return 1;
@@ -222,7 +216,7 @@ static int sweeps(GmlSct *gml, NatSct *n, GmlDatSct *ver, int ns, float omega)
    void *a = ver->GpuMem, *b = n->crd2;
    for(int s=0;s<ns;s++)
    {
-      if(!gmd_mesh_laplace(gml->dev, n->nv, n->soff, n->pdeg, n->pcol, a, b, omega))
+      if(!gmd_mesh_laplace(gml->dev, n->nv, n->pptr, n->pcol, a, b, omega))
          return 0;
       void *t = a; a = b; b = t;
    }
@@ -262,6 +256,17 @@ static void decode(const GmlxQualStats *s, GmlxQuality *r)
    memcpy(r->Hist, s->Hist, sizeof(r->Hist));
 }
 
+/* device error bits set by the kernels: 1 ball too large, 2 bad vertex
+   index, 4 a shared-memory staging copy did not arrive in time */
+static int device_errors(GmlSct *gml, NatSct *n)
+{
+   int err = 0;
+   gmd_d2h(gml->dev, &err, n->err, sizeof(int));
+   if(err & 4)
+      puts("GMlib: a quality-kernel staging copy timed out; statistics are incomplete.");
+   return err;
+}
+
 static float det_threshold(double h)
 {
    return (float)(1e-6 * h * h * h);
@@ -289,12 +294,12 @@ int GmlxQualityStats(size_t GmlIdx, double h, int QalIdx, GmlxQuality *res)
    gml_lib_timer_begin(gml, &gml->krn[ n->NmbQalKrn ]);
    gmd_mesh_stats_init(gml->dev, n->stats, 1);
    if(!gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, ver->GpuMem, det_threshold(h),
-                        q ? (float *)q->GpuMem : NULL, n->flags, n->stats))
+                        q ? (float *)q->GpuMem : NULL, n->flags, n->stats, n->err))
       return 0;
    gml_lib_timer_end(gml, &gml->krn[ n->NmbQalKrn ]);
    if(res)
    {
-      if(!gmd_d2h(gml->dev, &st, n->stats, sizeof(st)))
+      if(!gmd_d2h(gml->dev, &st, n->stats, sizeof(st)) || (device_errors(gml, n) & 4))
          return 0;
       decode(&st, res);
    }
@@ -335,9 +340,9 @@ int GmlxSmoothQualityLoop(size_t GmlIdx, int nsweeps, float omega, double h, Gml
       gmd_mesh_stats_init(gml->dev, n->stats, nsweeps);
       for(int s=0;s<nsweeps;s++)
       {
-         gmd_mesh_laplace(gml->dev, n->nv, n->soff, n->pdeg, n->pcol, a, b, omega);
+         gmd_mesh_laplace(gml->dev, n->nv, n->pptr, n->pcol, a, b, omega);
          gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, b, det_threshold(h), NULL, n->flags,
-                          n->stats + s);
+                          n->stats + s, n->err);
          void *t = a; a = b; b = t;
       }
       if(a != ver->GpuMem)
@@ -361,7 +366,8 @@ int GmlxSmoothQualityLoop(size_t GmlIdx, int nsweeps, float omega, double h, Gml
    if(res)
    {
       st = malloc((size_t)nsweeps * sizeof(GmlxQualStats));
-      if(!st || !gmd_d2h(gml->dev, st, n->stats, (size_t)nsweeps * sizeof(GmlxQualStats)))
+      if(!st || !gmd_d2h(gml->dev, st, n->stats, (size_t)nsweeps * sizeof(GmlxQualStats))
+      || (device_errors(gml, n) & 4))
       {
          free(st);
          return 0;
