@@ -463,20 +463,20 @@ __device__ __forceinline__ void tma_bulk_g2s(void *dst, const void *src, unsigne
                 :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
 
+/* non-blocking probe of the phase with the given parity */
 __device__ __forceinline__ int mbar_try_wait(unsigned long long *bar, unsigned parity)
 {
    unsigned ok;
    asm volatile("{\n\t.reg .pred p;\n\t"
-                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
                 "selp.u32 %0, 1, 0, p;\n\t}"
                 : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
    return (int)ok;
 }
 
-/* bounded wait: gives up after QK_SPIN polls (each try_wait may itself
-   suspend for a while), so a lost transfer ends the kernel instead of
-   hanging it */
-#define QK_SPIN (1 << 20)
+/* bounded wait: gives up after QK_SPIN polls (well under a second), so a
+   lost transfer ends the kernel with an error flag instead of hanging it */
+#define QK_SPIN (1 << 22)
 
 __device__ __forceinline__ int mbar_wait_bounded(unsigned long long *bar, unsigned parity)
 {
