@@ -158,7 +158,8 @@ __global__ void boundary_kernel(const int4 *__restrict__ tet, int nt, const int 
 
 #define PB_MAX 64
 #define PB_ROW_SHIFT 27
-#define PB_COL_MASK ((1 << PB_ROW_SHIFT) - 1)
+#define PB_COL_MASK ((1u << PB_ROW_SHIFT) - 1u)
+#define PB_NONE     0xffffffffu           /* no entry (a column never reaches 2^27 - 1) */
 
 /* distinct vertices of the tets around v, ascending; returns the count or
    -1 when the ball exceeds PB_MAX */
@@ -217,7 +218,7 @@ __global__ void point_fill_kernel(int nv, const int4 *__restrict__ tet, const in
    if(!d) return;
    int n = point_ball(v, tet, ptr, vt, lst);
    for(int k=0;k<n && k<d;k++)
-      pcol[ pptr[v] + k ] = ((v & 31) << PB_ROW_SHIFT) | lst[k];
+      pcol[ pptr[v] + k ] = (int)(((unsigned)(v & 31) << PB_ROW_SHIFT) | (unsigned)lst[k]);
 }
 
 /* ========================================================================= */
@@ -253,16 +254,16 @@ laplace_warp_kernel(int nv, const int *__restrict__ pptr, const int *__restrict_
    {
       /* two chunks of 32 entries in flight */
       const int ea = base + lane, eb = base + 32 + lane;
-      const int ka = ea < e1 ? __ldg(&pcol[ea]) : -1;
-      const int kb = eb < e1 ? __ldg(&pcol[eb]) : -1;
+      const unsigned ka = ea < e1 ? (unsigned)__ldg(&pcol[ea]) : PB_NONE;
+      const unsigned kb = eb < e1 ? (unsigned)__ldg(&pcol[eb]) : PB_NONE;
       float4 qa = make_float4(0.f, 0.f, 0.f, 0.f), qb = qa;
-      if(ka >= 0) qa = __ldg(&in[ ka & PB_COL_MASK ]);
-      if(kb >= 0) qb = __ldg(&in[ kb & PB_COL_MASK ]);
+      if(ka != PB_NONE) qa = __ldg(&in[ ka & PB_COL_MASK ]);
+      if(kb != PB_NONE) qb = __ldg(&in[ kb & PB_COL_MASK ]);
 #pragma unroll
       for(int h=0;h<2;h++)
       {
-         const int key = h ? kb : ka;
-         const int r = key >= 0 ? (key >> PB_ROW_SHIFT) : -1;
+         const unsigned key = h ? kb : ka;
+         const int r = key != PB_NONE ? (int)(key >> PB_ROW_SHIFT) : 32;
          float x = h ? qb.x : qa.x, y = h ? qb.y : qa.y, z = h ? qb.z : qa.z;
 #pragma unroll
          for(int o=1;o<32;o<<=1)
@@ -277,7 +278,7 @@ laplace_warp_kernel(int nv, const int *__restrict__ pptr, const int *__restrict_
             }
          }
          const int rn = __shfl_down_sync(0xffffffffu, r, 1);
-         if(r >= 0 && (lane == 31 || rn != r))
+         if(r < 32 && (lane == 31 || rn != r))
          {
             ax[r] += x; ay[r] += y; az[r] += z;
          }
