@@ -17,12 +17,16 @@ int gmd_mesh_vt_csr(struct GmdCtx *ctx, const void *tet, int nt, int nv,
                     int *ptr, int *vt, int *tmp, int *err);
 int gmd_mesh_boundary(struct GmdCtx *ctx, const void *tet, int nt, const int *ptr,
                       const int *vt, int *fixed);
+/* ball of points as SELL-C-sigma: rows are vertices sorted by ball size in
+   windows of 256 (rowv packs (size << 26) | vertex), slices of 32 rows */
+#define GML_SIGMA 256
 int gmd_mesh_point_count(struct GmdCtx *ctx, const void *tet, int nv, const int *ptr,
-                         const int *vt, const int *fixed, int *pdeg, int *pptr, int *err);
-int gmd_mesh_point_fill(struct GmdCtx *ctx, const void *tet, int nv, const int *ptr,
-                        const int *vt, const int *pptr, int *pcol);
-int gmd_mesh_laplace(struct GmdCtx *ctx, int nv, const int *pptr, const int *pcol,
-                     const void *in, void *out, float omega);
+                         const int *vt, const int *fixed, int *pdeg, unsigned *rowv,
+                         long long *width, long long *soff, int *err);
+int gmd_mesh_point_fill(struct GmdCtx *ctx, const void *tet, int nrow, const int *ptr,
+                        const int *vt, const unsigned *rowv, const long long *soff, int *col);
+int gmd_mesh_laplace(struct GmdCtx *ctx, int nrow, const unsigned *rowv, const long long *soff,
+                     const int *col, const void *in, void *out, float omega);
 int gmd_mesh_stats_init(struct GmdCtx *ctx, GmlxQualStats *st, int n);
 int gmd_mesh_quality(struct GmdCtx *ctx, int nt, const void *tet, const void *crd, float thr,
                      float *qout, unsigned *flags, GmlxQualStats *st, int *err);

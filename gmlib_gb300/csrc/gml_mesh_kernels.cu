@@ -8,18 +8,17 @@
  *                               fill (atomic slots; order within a ball is
  *                               not used by the kernels below)
  *   ball of points              per vertex, the distinct vertices of its
- *                               tetrahedra, sorted ascending, in CSR form;
- *                               each entry carries the row of its vertex
- *                               inside the vertex's group of 32; fixed
+ *                               tetrahedra, sorted ascending, stored as
+ *                               SELL-C-sigma (C = 32, sigma = 256: sorted by
+ *                               size inside windows of 256 vertices); fixed
  *                               vertices get an empty ball
  *   boundary vertices           vertices of faces owned by a single tet
  *
  * Hot kernels (HBM-bound):
- *   laplace_warp   one Jacobi sweep x' = x + w (mean(ball) - x), one warp
- *                  per 32 consecutive vertices; per vertex 4 (row pointer)
- *                  + 4 deg (entries, streamed in 128-byte runs) + 16 (own)
- *                  + 16 (write) bytes; neighbour gathers hit L2 (the
- *                  coordinates are 16 V bytes).
+ *   laplace_sell   one Jacobi sweep x' = x + w (mean(ball) - x), one thread
+ *                  per row; per vertex 4 (packed row word) + 4 deg (entries,
+ *                  128-byte runs per warp) + 16 (own) + 16 (write) bytes;
+ *                  neighbour gathers hit L2 (the coordinates are 16 V bytes).
  *   tet_quality    mean-ratio quality 12 (3|V|)^(2/3) / sum l^2 signed by
  *                  orientation, 64-bin histogram, min/argmin, max/argmax,
  *                  sum, inverted-element count and bit flags; the 16 bytes
@@ -153,13 +152,10 @@ __global__ void boundary_kernel(const int4 *__restrict__ tet, int nt, const int 
 }
 
 /* ========================================================================= */
-/* ball of points (CSR, entries tagged with the row inside its warp group)    */
+/* ball of points                                                             */
 /* ========================================================================= */
 
-#define PB_MAX 64
-#define PB_ROW_SHIFT 27
-#define PB_COL_MASK ((1u << PB_ROW_SHIFT) - 1u)
-#define PB_NONE     0xffffffffu           /* no entry (a column never reaches 2^27 - 1) */
+#define PB_MAX 63
 
 /* distinct vertices of the tets around v, ascending; returns the count or
    -1 when the ball exceeds PB_MAX */
@@ -204,102 +200,99 @@ __global__ void point_count_kernel(int nv, const int4 *__restrict__ tet, const i
    pdeg[v] = n;
 }
 
-/* entry = (v & 31) << 27 | neighbour: the row of v inside its group of 32
-   vertices travels with the column so that a warp can reduce a group's
-   contiguous entries without a search */
-__global__ void point_fill_kernel(int nv, const int4 *__restrict__ tet, const int *__restrict__ ptr,
-                                  const int *__restrict__ vt, const int *__restrict__ pptr,
-                                  int *pcol)
+/* SELL-C-sigma layout of the balls of points.  Vertices are sorted by
+   decreasing ball size inside windows of SIGMA consecutive vertices (the
+   Hilbert locality of the numbering is kept), rows are grouped by 32 into
+   slices as wide as their first row, and entry k of the 32 rows of a slice
+   is stored contiguously.  rowv[r] packs the vertex of row r and its ball
+   size: (d << 26) | v.  One thread per row then streams column indices in
+   128-byte runs with almost no padding. */
+#define SIGMA      256
+#define ROW_SHIFT  26
+#define ROW_MASK   ((1u << ROW_SHIFT) - 1u)
+#define ROW_NONE   0xffffffffu
+
+__global__ void __launch_bounds__(SIGMA)
+window_sort_kernel(int nv, const int *__restrict__ pdeg, unsigned *rowv)
 {
-   int v = blockIdx.x * blockDim.x + threadIdx.x;
+   __shared__ int dd[SIGMA];
+   const int t = threadIdx.x, v = blockIdx.x * SIGMA + t;
+   const int d = v < nv ? pdeg[v] : -1;
+   dd[t] = d;
+   __syncthreads();
+   int rank = 0;
+   for(int u=0;u<SIGMA;u++)
+   {
+      const int du = dd[u];
+      rank += (du > d) || (du == d && u < t);
+   }
+   rowv[ blockIdx.x * SIGMA + rank ] = v < nv ? (((unsigned)d << ROW_SHIFT) | (unsigned)v) : ROW_NONE;
+}
+
+__global__ void slice_width_kernel(int nslice, const unsigned *__restrict__ rowv, long long *w)
+{
+   const int s = blockIdx.x * blockDim.x + threadIdx.x;
+   if(s >= nslice) return;
+   const unsigned r = rowv[ 32 * s ];
+   w[s] = r == ROW_NONE ? 0 : (long long)(r >> ROW_SHIFT);
+}
+
+__global__ void point_fill_kernel(int nrow, const int4 *__restrict__ tet, const int *__restrict__ ptr,
+                                  const int *__restrict__ vt, const unsigned *__restrict__ rowv,
+                                  const long long *__restrict__ soff, int *col)
+{
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
    int lst[PB_MAX];
-   if(v >= nv) return;
-   int d = pptr[v+1] - pptr[v];
-   if(!d) return;
-   int n = point_ball(v, tet, ptr, vt, lst);
+   if(r >= nrow) return;
+   const unsigned pk = rowv[r];
+   if(pk == ROW_NONE || !(pk >> ROW_SHIFT)) return;
+   const int v = (int)(pk & ROW_MASK), d = (int)(pk >> ROW_SHIFT);
+   const int n = point_ball(v, tet, ptr, vt, lst);
+   const long long base = soff[ r >> 5 ];
    for(int k=0;k<n && k<d;k++)
-      pcol[ pptr[v] + k ] = (int)(((unsigned)(v & 31) << PB_ROW_SHIFT) | (unsigned)lst[k]);
+      col[ (base + k) * 32 + (r & 31) ] = lst[k];
 }
 
 /* ========================================================================= */
-/* Laplacian sweep: one warp per group of 32 consecutive vertices             */
+/* Laplacian sweep over the ball of points, one thread per SELL row           */
 /* ========================================================================= */
 
-/* The group's entries are contiguous in the CSR arrays; the warp streams
-   them 32 at a time (coalesced 128-byte column loads, 32 independent
-   coordinate gathers), sums each row's run with a shuffle segmented scan
-   whose tail lane adds into shared memory (one writer per row and chunk,
-   chunks in order: the summation order is fixed, results are
-   reproducible), then lane r updates vertex 32g + r. */
 __global__ void __launch_bounds__(MK_THREADS)
-laplace_warp_kernel(int nv, const int *__restrict__ pptr, const int *__restrict__ pcol,
-                    const float4 *__restrict__ in, float4 *__restrict__ out, float omega)
+laplace_sell_kernel(int nrow, const unsigned *__restrict__ rowv, const long long *__restrict__ soff,
+                    const int *__restrict__ col, const float4 *__restrict__ in,
+                    float4 *__restrict__ out, float omega)
 {
-   __shared__ float acc[MK_THREADS / 32][3][32];
-   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-   const int v0 = (blockIdx.x * MK_THREADS + threadIdx.x) & ~31;
-   if(v0 >= nv)
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if(r >= nrow) return;
+   const unsigned pk = __ldg(&rowv[r]);
+   if(pk == ROW_NONE) return;
+   const int v = (int)(pk & ROW_MASK), d = (int)(pk >> ROW_SHIFT);
+   const float4 p = __ldg(&in[v]);
+   if(d == 0)
+   {
+      out[v] = p;
       return;
-   const int v = v0 + lane;
-   const int vl = v < nv ? v : nv;
-   const int e0 = __ldg(&pptr[v0]);
-   const int p0 = __ldg(&pptr[vl]), p1 = __ldg(&pptr[v < nv ? v + 1 : nv]);
-   const int e1 = __shfl_sync(0xffffffffu, p1, 31);
-   float *ax = acc[wid][0], *ay = acc[wid][1], *az = acc[wid][2];
-
-   ax[lane] = 0.f; ay[lane] = 0.f; az[lane] = 0.f;
-   __syncwarp();
-
-   for(int base=e0; base<e1; base+=64)
-   {
-      /* two chunks of 32 entries in flight */
-      const int ea = base + lane, eb = base + 32 + lane;
-      const unsigned ka = ea < e1 ? (unsigned)__ldg(&pcol[ea]) : PB_NONE;
-      const unsigned kb = eb < e1 ? (unsigned)__ldg(&pcol[eb]) : PB_NONE;
-      float4 qa = make_float4(0.f, 0.f, 0.f, 0.f), qb = qa;
-      if(ka != PB_NONE) qa = __ldg(&in[ ka & PB_COL_MASK ]);
-      if(kb != PB_NONE) qb = __ldg(&in[ kb & PB_COL_MASK ]);
-#pragma unroll
-      for(int h=0;h<2;h++)
-      {
-         const unsigned key = h ? kb : ka;
-         const int r = key != PB_NONE ? (int)(key >> PB_ROW_SHIFT) : 32;
-         float x = h ? qb.x : qa.x, y = h ? qb.y : qa.y, z = h ? qb.z : qa.z;
-#pragma unroll
-         for(int o=1;o<32;o<<=1)
-         {
-            const float xo = __shfl_up_sync(0xffffffffu, x, o);
-            const float yo = __shfl_up_sync(0xffffffffu, y, o);
-            const float zo = __shfl_up_sync(0xffffffffu, z, o);
-            const int ro = __shfl_up_sync(0xffffffffu, r, o);
-            if(lane >= o && ro == r)
-            {
-               x += xo; y += yo; z += zo;
-            }
-         }
-         const int rn = __shfl_down_sync(0xffffffffu, r, 1);
-         if(r < 32 && (lane == 31 || rn != r))
-         {
-            ax[r] += x; ay[r] += y; az[r] += z;
-         }
-         __syncwarp();
-      }
    }
-
-   if(v < nv)
+   const int *cp = col + __ldg(&soff[r >> 5]) * 32 + (r & 31);
+   float sx = 0.f, sy = 0.f, sz = 0.f;
+   int k = 0;
+   for(;k+4<=d;k+=4)
    {
-      const float4 p = __ldg(&in[v]);
-      const int d = p1 - p0;
-      if(d == 0)
-         out[v] = p;
-      else
-      {
-         const float inv = 1.0f / (float)d;
-         out[v] = make_float4(p.x + omega * (ax[lane] * inv - p.x),
-                              p.y + omega * (ay[lane] * inv - p.y),
-                              p.z + omega * (az[lane] * inv - p.z), 0.f);
-      }
+      const int c0 = __ldg(cp + (size_t)k * 32), c1 = __ldg(cp + (size_t)(k + 1) * 32);
+      const int c2 = __ldg(cp + (size_t)(k + 2) * 32), c3 = __ldg(cp + (size_t)(k + 3) * 32);
+      const float4 q0 = __ldg(&in[c0]), q1 = __ldg(&in[c1]), q2 = __ldg(&in[c2]), q3 = __ldg(&in[c3]);
+      sx += (q0.x + q1.x) + (q2.x + q3.x);
+      sy += (q0.y + q1.y) + (q2.y + q3.y);
+      sz += (q0.z + q1.z) + (q2.z + q3.z);
    }
+   for(;k<d;k++)
+   {
+      const float4 q = __ldg(&in[ __ldg(cp + (size_t)k * 32) ]);
+      sx += q.x; sy += q.y; sz += q.z;
+   }
+   const float inv = 1.0f / (float)d;
+   out[v] = make_float4(p.x + omega * (sx * inv - p.x), p.y + omega * (sy * inv - p.y),
+                        p.z + omega * (sz * inv - p.z), 0.f);
 }
 
 /* ========================================================================= */
@@ -310,6 +303,14 @@ __device__ __forceinline__ unsigned mk_fkey(float f)
 {
    unsigned u = __float_as_uint(f);
    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+/* 2^x on the special-function unit (ex2.approx.ftz.f32) */
+__device__ __forceinline__ float exp2f_fast(float x)
+{
+   float y;
+   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+   return y;
 }
 
 __global__ void stats_init_kernel(GmlxQualStats *st, int n)
@@ -327,8 +328,10 @@ __global__ void stats_init_kernel(GmlxQualStats *st, int n)
 }
 
 /* signed mean-ratio quality of one tet; *inv = det <= 0 (FP64 sign when the
-   FP32 determinant is below the threshold or its error bound), *f64 = 1
-   when the FP64 determinant was used */
+   FP32 determinant is below the threshold or below a bound of its own
+   rounding error), *f64 = 1 when the FP64 determinant was used.
+   q = 12 (|det|/2)^(2/3) / l2 is evaluated with the special-function unit
+   (log2/exp2, about 2^-22 relative error) and a fast reciprocal. */
 __device__ __forceinline__ float tet_mean_ratio(const int4 e, const float4 *__restrict__ crd,
                                                 float thr, int *inv, int *f64)
 {
@@ -337,14 +340,15 @@ __device__ __forceinline__ float tet_mean_ratio(const int4 e, const float4 *__re
    const float abx = b.x - a.x, aby = b.y - a.y, abz = b.z - a.z;
    const float acx = c.x - a.x, acy = c.y - a.y, acz = c.z - a.z;
    const float adx = d.x - a.x, ady = d.y - a.y, adz = d.z - a.z;
-   const float m1 = acy * adz - acz * ady, m2 = acz * adx - acx * adz, m3 = acx * ady - acy * adx;
-   float det = abx * m1 + aby * m2 + abz * m3;
+   float det = abx * (acy * adz - acz * ady) + aby * (acz * adx - acx * adz)
+             + abz * (acx * ady - acy * adx);
    int pos = det > 0.f;
-   const float perm = fabsf(abx) * (fabsf(acy * adz) + fabsf(acz * ady))
-                    + fabsf(aby) * (fabsf(acz * adx) + fabsf(acx * adz))
-                    + fabsf(abz) * (fabsf(acx * ady) + fabsf(acy * adx));
+   /* |det| error bound: 16 eps32 times a product that dominates the sum of
+      the absolute values of the six products of the expansion */
+   const float bnd = (fabsf(abx) + fabsf(aby) + fabsf(abz)) * (fabsf(acx) + fabsf(acy) + fabsf(acz))
+                   * (fabsf(adx) + fabsf(ady) + fabsf(adz));
    *f64 = 0;
-   if(fabsf(det) < fmaxf(thr, 9.5367431640625e-07f * perm))
+   if(fabsf(det) < fmaxf(thr, 9.5367431640625e-07f * bnd))
    {
       const double Ax = a.x, Ay = a.y, Az = a.z;
       const double bx = b.x - Ax, by = b.y - Ay, bz = b.z - Az;
@@ -355,40 +359,46 @@ __device__ __forceinline__ float tet_mean_ratio(const int4 e, const float4 *__re
       pos = dd > 0.;
       *f64 = 1;
    }
-   const float bcx = c.x - b.x, bcy = c.y - b.y, bcz = c.z - b.z;
-   const float bdx = d.x - b.x, bdy = d.y - b.y, bdz = d.z - b.z;
-   const float cdx = d.x - c.x, cdy = d.y - c.y, cdz = d.z - c.z;
+   const float bcx = acx - abx, bcy = acy - aby, bcz = acz - abz;
+   const float bdx = adx - abx, bdy = ady - aby, bdz = adz - abz;
+   const float cdx = adx - acx, cdy = ady - acy, cdz = adz - acz;
    const float l2 = abx*abx + aby*aby + abz*abz + acx*acx + acy*acy + acz*acz
                   + adx*adx + ady*ady + adz*adz + bcx*bcx + bcy*bcy + bcz*bcz
                   + bdx*bdx + bdy*bdy + bdz*bdz + cdx*cdx + cdy*cdy + cdz*cdz;
-   const float cb = cbrtf(0.5f * fabsf(det));          /* (3 |det| / 6)^(1/3) */
-   const float q = 12.0f * cb * cb / l2;
+   const float v23 = exp2f_fast(0.6666666865f * __log2f(0.5f * fabsf(det)));
+   const float q = 12.0f * v23 * __frcp_rn(l2);
    *inv = !pos;
    return pos ? q : -q;
 }
 
-/* per-thread accumulators of the statistics */
+/* per-thread accumulators of the statistics (a thread sees its tets in
+   increasing index order, so strict comparisons keep the smallest index) */
 struct QAcc
 {
-   unsigned long long kmin, kmax;
-   float s, c;
+   float mn, mx, s, c;
+   int mi, xi;
    unsigned ninv, nf64;
 };
 
-__device__ __forceinline__ void qacc_add(QAcc &a, float q, int t, int f64, unsigned *hist)
+__device__ __forceinline__ void qacc_add(QAcc &a, float q, int t, int f64)
 {
-   int bin = (int)(q * 64.0f);
-   bin = bin < 0 ? 0 : (bin > 63 ? 63 : bin);
-   atomicAdd(&hist[bin], 1u);
-   const unsigned k = mk_fkey(q);
-   const unsigned long long a64 = ((unsigned long long)k << 32) | (unsigned)t;
-   const unsigned long long b64 = ((unsigned long long)(~k) << 32) | (unsigned)t;
-   a.kmin = a64 < a.kmin ? a64 : a.kmin;
-   a.kmax = b64 < a.kmax ? b64 : a.kmax;
+   if(q < a.mn) { a.mn = q; a.mi = t; }
+   if(q > a.mx) { a.mx = q; a.xi = t; }
    const float tt = a.s + q, bp = tt - a.s;
    a.c += (a.s - (tt - bp)) + (q - bp);
    a.s = tt;
    a.nf64 += f64;
+}
+
+/* histogram update of a warp: lanes with the same bin add once */
+__device__ __forceinline__ void hist_add_warp(unsigned *hist, float q, int valid, int lane)
+{
+   int bin = (int)(q * 64.0f);
+   bin = bin < 0 ? 0 : (bin > 63 ? 63 : bin);
+   if(!valid) bin = 64 + lane;
+   const unsigned peers = __match_any_sync(0xffffffffu, bin);
+   if(valid && lane == __ffs(peers) - 1)
+      atomicAdd(&hist[bin], (unsigned)__popc(peers));
 }
 
 /* block reduction of the accumulators into the global statistics */
@@ -399,9 +409,15 @@ __device__ __forceinline__ void qacc_flush(QAcc &a, unsigned *hist, GmlxQualStat
    __shared__ unsigned sinv[MK_THREADS / 32], sf64[MK_THREADS / 32];
    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
    double dsum = (double)a.s + (double)a.c;
-   unsigned long long kmin = a.kmin, kmax = a.kmax;
+   unsigned long long kmin = ~0ULL, kmax = ~0ULL;
    unsigned ninv = a.ninv, nf64 = a.nf64;
 
+   if(a.mi >= 0)
+   {
+      const unsigned k = mk_fkey(a.mn), kx = mk_fkey(a.mx);
+      kmin = ((unsigned long long)k << 32) | (unsigned)a.mi;
+      kmax = ((unsigned long long)(~kx) << 32) | (unsigned)a.xi;
+   }
    for(int o=16;o>0;o>>=1)
    {
       unsigned long long x = __shfl_xor_sync(0xffffffffu, kmin, o);
@@ -508,7 +524,7 @@ tet_quality_tma_kernel(int nt, const int4 *__restrict__ tet, const float4 *__res
    const int nchunk = (nt + QK_CHUNK - 1) / QK_CHUNK;
    const int mine = blockIdx.x < nchunk ? (nchunk - 1 - blockIdx.x) / gridDim.x + 1 : 0;
    int4 *stage = (int4 *)qk_smem;
-   QAcc a = { ~0ULL, ~0ULL, 0.f, 0.f, 0u, 0u };
+   QAcc a = { 3.402823466e38f, -3.402823466e38f, 0.f, 0.f, -1, -1, 0u, 0u };
 
    if(threadIdx.x < 64)
       hist[threadIdx.x] = 0;
@@ -561,14 +577,16 @@ tet_quality_tma_kernel(int nt, const int4 *__restrict__ tet, const float4 *__res
          if(j1 < n) q1 = tet_mean_ratio(chunk[j1], crd, thr, &inv1, &f1);
          if(j0 < n)
          {
-            qacc_add(a, q0, start + j0, f0, hist);
+            qacc_add(a, q0, start + j0, f0);
             if(qout) qout[start + j0] = q0;
          }
          if(j1 < n)
          {
-            qacc_add(a, q1, start + j1, f1, hist);
+            qacc_add(a, q1, start + j1, f1);
             if(qout) qout[start + j1] = q1;
          }
+         hist_add_warp(hist, q0, j0 < n, lane);
+         hist_add_warp(hist, q1, j1 < n, lane);
          const unsigned w0 = __ballot_sync(0xffffffffu, inv0);
          const unsigned w1 = __ballot_sync(0xffffffffu, inv1);
          if(lane == 0)
@@ -621,28 +639,32 @@ extern "C" int gmd_mesh_boundary(GmdCtx *ctx, const void *tet, int nt, const int
 }
 
 extern "C" int gmd_mesh_point_count(GmdCtx *ctx, const void *tet, int nv, const int *ptr,
-                                    const int *vt, const int *fixed, int *pdeg, int *pptr,
-                                    int *err)
+                                    const int *vt, const int *fixed, int *pdeg, unsigned *rowv,
+                                    long long *width, long long *soff, int *err)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   const int nwin = (nv + SIGMA - 1) / SIGMA, nslice = nwin * (SIGMA / 32);
    point_count_kernel<<<nblk(nv, 128), 128, 0, st>>>(nv, (const int4 *)tet, ptr, vt, fixed, pdeg, err);
-   scan_excl_kernel<int><<<1, 1024, 0, st>>>(pdeg, pptr, nv);
+   window_sort_kernel<<<nwin, SIGMA, 0, st>>>(nv, pdeg, rowv);
+   slice_width_kernel<<<nblk(nslice, MK_THREADS), MK_THREADS, 0, st>>>(nslice, rowv, width);
+   scan_excl_kernel<long long><<<1, 1024, 0, st>>>(width, soff, nslice);
    return cudaGetLastError() == cudaSuccess;
 }
 
-extern "C" int gmd_mesh_point_fill(GmdCtx *ctx, const void *tet, int nv, const int *ptr,
-                                   const int *vt, const int *pptr, int *pcol)
+extern "C" int gmd_mesh_point_fill(GmdCtx *ctx, const void *tet, int nrow, const int *ptr,
+                                   const int *vt, const unsigned *rowv, const long long *soff,
+                                   int *col)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
-   point_fill_kernel<<<nblk(nv, 128), 128, 0, st>>>(nv, (const int4 *)tet, ptr, vt, pptr, pcol);
+   point_fill_kernel<<<nblk(nrow, 128), 128, 0, st>>>(nrow, (const int4 *)tet, ptr, vt, rowv, soff, col);
    return cudaGetLastError() == cudaSuccess;
 }
 
-extern "C" int gmd_mesh_laplace(GmdCtx *ctx, int nv, const int *pptr, const int *pcol,
-                                const void *in, void *out, float omega)
+extern "C" int gmd_mesh_laplace(GmdCtx *ctx, int nrow, const unsigned *rowv, const long long *soff,
+                                const int *col, const void *in, void *out, float omega)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
-   laplace_warp_kernel<<<nblk(nv, MK_THREADS), MK_THREADS, 0, st>>>(nv, pptr, pcol,
+   laplace_sell_kernel<<<nblk(nrow, MK_THREADS), MK_THREADS, 0, st>>>(nrow, rowv, soff, col,
       (const float4 *)in, (float4 *)out, omega);
    return cudaGetLastError() == cudaSuccess;
 }

@@ -14,8 +14,11 @@
 typedef struct
 {
    int         nv, nt, fix, ready;
-   int         *ptr, *vt, *tmp, *err, *fixed, *pdeg, *pptr, *pcol;
-   long long   used;
+   int         nrow;                  /* rows of the SELL layout (windows x 256) */
+   int         *ptr, *vt, *tmp, *err, *fixed, *pdeg, *pcol;
+   unsigned    *rowv;
+   long long   *width, *soff;
+   long long   used, stored;
    int         maxdeg;
    void        *crd2;                 /* second coordinate buffer */
    unsigned    *flags;                /* inverted-element bits */
@@ -44,7 +47,8 @@ static void free_state(GmlSct *gml, NatSct *n)
    gmd_free(gml->dev, n->ptr);   gmd_free(gml->dev, n->vt);
    gmd_free(gml->dev, n->tmp);   gmd_free(gml->dev, n->err);
    gmd_free(gml->dev, n->fixed); gmd_free(gml->dev, n->pdeg);
-   gmd_free(gml->dev, n->pcol);  gmd_free(gml->dev, n->pptr);
+   gmd_free(gml->dev, n->pcol);  gmd_free(gml->dev, n->rowv);
+   gmd_free(gml->dev, n->width); gmd_free(gml->dev, n->soff);
    gmd_free(gml->dev, n->crd2);
    gmd_free(gml->dev, n->flags); gmd_free(gml->dev, n->stats);
    gmd_graph_free(n->graph);
@@ -78,7 +82,8 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
    GETGMLPTR(gml, GmlIdx);
    GmlDatSct *ver, *tet;
    NatSct *n;
-   int nv, nt, err = 0, *pdeg_h, tot;
+   int nv, nt, err = 0, *pdeg_h, nslice;
+   long long tot;
 
    if(gml->Offline || !mesh_dat(gml, &ver, &tet))
       return 0;
@@ -87,12 +92,14 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
    free_state(gml, n);
    nv = ver->NmbLin;
    nt = tet->NmbLin;
-   if(nv >= (1 << 27))
+   if(nv >= (1 << 26))
    {
-      puts("GmlxMeshSetup: more than 2^27 vertices");
+      puts("GmlxMeshSetup: more than 2^26 vertices");
       return 0;
    }
    n->nv = nv;
+   n->nrow = ((nv + GML_SIGMA - 1) / GML_SIGMA) * GML_SIGMA;
+   nslice = n->nrow / 32;
    n->nt = nt;
    n->fix = fix;
 
@@ -101,13 +108,15 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
    n->tmp   = gmd_alloc(gml->dev, (size_t)nv * sizeof(int));
    n->err   = gmd_alloc(gml->dev, sizeof(int));
    n->pdeg  = gmd_alloc(gml->dev, (size_t)nv * sizeof(int));
-   n->pptr  = gmd_alloc(gml->dev, (size_t)(nv + 1) * sizeof(int));
+   n->rowv  = gmd_alloc(gml->dev, (size_t)n->nrow * sizeof(unsigned));
+   n->width = gmd_alloc(gml->dev, (size_t)(nslice + 1) * sizeof(long long));
+   n->soff  = gmd_alloc(gml->dev, (size_t)(nslice + 1) * sizeof(long long));
    n->crd2  = gmd_alloc(gml->dev, (size_t)nv * 16);
    n->flags = gmd_alloc(gml->dev, (size_t)((nt + 31) / 32) * sizeof(unsigned));
    n->stats = gmd_alloc(gml->dev, GML_MAXSTATS * sizeof(GmlxQualStats));
    n->nstats = GML_MAXSTATS;
-   if(!n->ptr || !n->vt || !n->tmp || !n->err || !n->pdeg || !n->pptr
-   || !n->crd2 || !n->flags || !n->stats)
+   if(!n->ptr || !n->vt || !n->tmp || !n->err || !n->pdeg || !n->rowv || !n->width
+   || !n->soff || !n->crd2 || !n->flags || !n->stats)
    {
       free_state(gml, n);
       return 0;
@@ -140,7 +149,7 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
    }
 
    gmd_mesh_point_count(gml->dev, tet->GpuMem, nv, n->ptr, n->vt, n->fixed, n->pdeg,
-                        n->pptr, n->err);
+                        n->rowv, n->width, n->soff, n->err);
 
    pdeg_h = malloc((size_t)nv * sizeof(int));
    if(!pdeg_h)
@@ -149,31 +158,35 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
       return 0;
    }
    gmd_d2h(gml->dev, &err, n->err, sizeof(int));
-   gmd_d2h(gml->dev, &tot, n->pptr + nv, sizeof(int));
+   gmd_d2h(gml->dev, &tot, n->soff + nslice, sizeof(long long));
    gmd_d2h(gml->dev, pdeg_h, n->pdeg, (size_t)nv * sizeof(int));
 
    if(err)
    {
       printf("GmlxMeshSetup: %s\n", (err & 2) ? "vertex index out of range in the tetrahedra"
-                                               : "a ball of points exceeds 64 vertices");
+                                               : "a ball of points exceeds 63 vertices");
       free(pdeg_h);
       free_state(gml, n);
       return 0;
    }
 
-   n->used = tot;
+   n->stored = tot * 32;
+   n->used = 0;
    n->maxdeg = 0;
    for(int i=0;i<nv;i++)
+   {
+      n->used += pdeg_h[i];
       if(pdeg_h[i] > n->maxdeg) n->maxdeg = pdeg_h[i];
+   }
    free(pdeg_h);
 
-   n->pcol = gmd_alloc(gml->dev, (size_t)(tot > 0 ? tot : 1) * sizeof(int));
+   n->pcol = gmd_alloc(gml->dev, (size_t)(tot > 0 ? tot : 1) * 32 * sizeof(int));
    if(!n->pcol)
    {
       free_state(gml, n);
       return 0;
    }
-   gmd_mesh_point_fill(gml->dev, tet->GpuMem, nv, n->ptr, n->vt, n->pptr, n->pcol);
+   gmd_mesh_point_fill(gml->dev, tet->GpuMem, n->nrow, n->ptr, n->vt, n->rowv, n->soff, n->pcol);
    gmd_sync(gml->dev);
    n->ready = 1;
    return 1;
@@ -185,7 +198,7 @@ int GmlxMeshBallInfo(size_t GmlIdx, long long *stored, long long *used, int *max
    NatSct *n = gml->ext;
    if(!n || !n->ready)
       return 0;
-   if(stored) *stored = n->used;
+   if(stored) *stored = n->stored;
    if(used) *used = n->used;
    if(maxdeg) *maxdeg = n->maxdeg;
    return 1;
@@ -216,7 +229,7 @@ static int sweeps(GmlSct *gml, NatSct *n, GmlDatSct *ver, int ns, float omega)
    void *a = ver->GpuMem, *b = n->crd2;
    for(int s=0;s<ns;s++)
    {
-      if(!gmd_mesh_laplace(gml->dev, n->nv, n->pptr, n->pcol, a, b, omega))
+      if(!gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, a, b, omega))
          return 0;
       void *t = a; a = b; b = t;
    }
@@ -340,7 +353,7 @@ int GmlxSmoothQualityLoop(size_t GmlIdx, int nsweeps, float omega, double h, Gml
       gmd_mesh_stats_init(gml->dev, n->stats, nsweeps);
       for(int s=0;s<nsweeps;s++)
       {
-         gmd_mesh_laplace(gml->dev, n->nv, n->pptr, n->pcol, a, b, omega);
+         gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, a, b, omega);
          gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, b, det_threshold(h), NULL, n->flags,
                           n->stats + s, n->err);
          void *t = a; a = b; b = t;
