@@ -26,7 +26,7 @@ int gmd_mesh_point_count(struct GmdCtx *ctx, const void *tet, int nv, const int 
 int gmd_mesh_point_fill(struct GmdCtx *ctx, const void *tet, int nrow, const int *ptr,
                         const int *vt, const unsigned *rowv, const long long *soff, int *col);
 int gmd_mesh_laplace(struct GmdCtx *ctx, int nrow, const unsigned *rowv, const long long *soff,
-                     const int *col, const void *in, void *out, float omega);
+                     const int *col, const void *in, void *out, float omega, int *err);
 int gmd_mesh_stats_init(struct GmdCtx *ctx, GmlxQualStats *st, int n);
 int gmd_mesh_quality(struct GmdCtx *ctx, int nt, const void *tet, const void *crd, float thr,
                      float *qout, unsigned *flags, GmlxQualStats *st, int *err);

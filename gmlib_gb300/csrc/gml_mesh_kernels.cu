@@ -212,6 +212,56 @@ __global__ void point_count_kernel(int nv, const int4 *__restrict__ tet, const i
 #define ROW_MASK   ((1u << ROW_SHIFT) - 1u)
 #define ROW_NONE   0xffffffffu
 
+/* ------------------------------------------------------------------------- */
+/* TMA bulk copies and mbarriers (inline PTX)                                 */
+/* ------------------------------------------------------------------------- */
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+   return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                             unsigned long long *bar)
+{
+   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+/* non-blocking probe of the phase with the given parity */
+__device__ __forceinline__ int mbar_try_wait(unsigned long long *bar, unsigned parity)
+{
+   unsigned ok;
+   asm volatile("{\n\t.reg .pred p;\n\t"
+                "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+   return (int)ok;
+}
+
+/* bounded wait: gives up after QK_SPIN polls (well under a second), so a
+   lost transfer ends the kernel with an error flag instead of hanging it */
+#define QK_SPIN (1 << 22)
+
+__device__ __forceinline__ int mbar_wait_bounded(unsigned long long *bar, unsigned parity)
+{
+   for(int i=0;i<QK_SPIN;i++)
+      if(mbar_try_wait(bar, parity))
+         return 1;
+   return 0;
+}
+
 __global__ void __launch_bounds__(SIGMA)
 window_sort_kernel(int nv, const int *__restrict__ pdeg, unsigned *rowv)
 {
@@ -295,6 +345,126 @@ laplace_sell_kernel(int nrow, const unsigned *__restrict__ rowv, const long long
                         p.z + omega * (sz * inv - p.z), 0.f);
 }
 
+/* The same sweep with the column block of each 256-row tile (8 slices,
+   contiguous in the SELL arrays) staged into shared memory by a TMA bulk
+   copy issued one tile ahead, so that the column stream never sits on the
+   gather chain: each thread reads its indices from shared memory and issues
+   its coordinate gathers back to back.  Tiles whose block exceeds the stage
+   capacity (balls wider than 32 on average in the tile) read their columns
+   from global memory instead. */
+#define LT_ROWS   SIGMA                       /* rows per tile */
+#define LT_CAP    (32 * 32 * (LT_ROWS / 32))  /* ints per stage: width <= 32 */
+#define LT_STAGES 2
+#define LT_SMEM   (LT_STAGES * LT_CAP * 4)
+
+__global__ void __launch_bounds__(LT_ROWS, 3)
+laplace_tma_kernel(int ntile, const unsigned *__restrict__ rowv, const long long *__restrict__ soff,
+                   const int *__restrict__ col, const float4 *__restrict__ in,
+                   float4 *__restrict__ out, float omega, int *err)
+{
+   extern __shared__ __align__(128) unsigned char lt_smem[];
+   __shared__ __align__(8) unsigned long long bar[LT_STAGES];
+   __shared__ long long toff[LT_STAGES][LT_ROWS / 32 + 1];
+   int *stage = (int *)lt_smem;
+   const int tid = threadIdx.x, lane = tid & 31, sl = tid >> 5;
+   const int mine = blockIdx.x < ntile ? (ntile - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+
+   /* thread 0 issues the copy of local tile i into stage i % LT_STAGES */
+   #define LT_ISSUE(i)                                                            \
+   {                                                                              \
+      const int tt = blockIdx.x + (i) * gridDim.x, ss = (i) % LT_STAGES;          \
+      const long long c0 = soff[ tt * (LT_ROWS / 32) ];                           \
+      const long long c1 = soff[ tt * (LT_ROWS / 32) + LT_ROWS / 32 ];            \
+      const unsigned bytes = (unsigned)((c1 - c0) * 128);                         \
+      if(bytes && bytes <= LT_CAP * 4)                                            \
+      {                                                                           \
+         mbar_expect_tx(&bar[ss], bytes);                                         \
+         tma_bulk_g2s(stage + ss * LT_CAP, col + c0 * 32, bytes, &bar[ss]);       \
+      }                                                                           \
+      else                                                                        \
+         mbar_expect_tx(&bar[ss], 0);                                             \
+   }
+
+   if(tid == 0)
+   {
+      for(int s=0;s<LT_STAGES;s++)
+         mbar_init(&bar[s], 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      for(int i=0;i<LT_STAGES && i<mine;i++)
+         LT_ISSUE(i);
+   }
+   __syncthreads();
+
+   for(int i=0;i<mine;i++)
+   {
+      const int t = blockIdx.x + i * gridDim.x, s = i % LT_STAGES;
+      const unsigned parity = (unsigned)((i / LT_STAGES) & 1);
+      if(tid <= LT_ROWS / 32)
+         toff[s][tid] = __ldg(&soff[ t * (LT_ROWS / 32) + tid ]);
+      const int r = t * LT_ROWS + tid;
+      const unsigned pk = __ldg(&rowv[r]);
+      const int ok = mbar_wait_bounded(&bar[s], parity);
+      if(__syncthreads_or(!ok))
+      {
+         if(tid == 0)
+         {
+            atomicOr(err, 8);
+            for(int j=i;j<mine && j<i+LT_STAGES;j++)
+               mbar_wait_bounded(&bar[j % LT_STAGES], (unsigned)((j / LT_STAGES) & 1));
+         }
+         __syncthreads();
+         return;
+      }
+
+      if(pk != ROW_NONE)
+      {
+         const int v = (int)(pk & ROW_MASK), d = (int)(pk >> ROW_SHIFT);
+         const float4 p = __ldg(&in[v]);
+         if(d == 0)
+            out[v] = p;
+         else
+         {
+            const long long base = toff[s][0];
+            const bool staged = (toff[s][LT_ROWS / 32] - base) * 32 <= LT_CAP;
+            const int *cp = staged ? stage + s * LT_CAP + (toff[s][sl] - base) * 32 + lane
+                                   : col + toff[s][sl] * 32 + lane;
+            float sx = 0.f, sy = 0.f, sz = 0.f;
+            int k = 0;
+            for(;k+8<=d;k+=8)
+            {
+               int c[8];
+               float4 q[8];
+#pragma unroll
+               for(int u=0;u<8;u++)
+                  c[u] = cp[(k + u) * 32];
+#pragma unroll
+               for(int u=0;u<8;u++)
+                  q[u] = __ldg(&in[ c[u] ]);
+#pragma unroll
+               for(int u=0;u<8;u++)
+               {
+                  sx += q[u].x; sy += q[u].y; sz += q[u].z;
+               }
+            }
+            for(;k<d;k++)
+            {
+               const float4 q = __ldg(&in[ cp[k * 32] ]);
+               sx += q.x; sy += q.y; sz += q.z;
+            }
+            const float inv = 1.0f / (float)d;
+            out[v] = make_float4(p.x + omega * (sx * inv - p.x), p.y + omega * (sy * inv - p.y),
+                                 p.z + omega * (sz * inv - p.z), 0.f);
+         }
+      }
+
+      /* all reads of stage s done: refill it with tile i + LT_STAGES */
+      __syncthreads();
+      if(tid == 0 && i + LT_STAGES < mine)
+         LT_ISSUE(i + LT_STAGES);
+   }
+   #undef LT_ISSUE
+}
+
 /* ========================================================================= */
 /* mean-ratio quality, histogram, extrema, inverted flags                     */
 /* ========================================================================= */
@@ -366,7 +536,7 @@ __device__ __forceinline__ float tet_mean_ratio(const int4 e, const float4 *__re
                   + adx*adx + ady*ady + adz*adz + bcx*bcx + bcy*bcy + bcz*bcz
                   + bdx*bdx + bdy*bdy + bdz*bdz + cdx*cdx + cdy*cdy + cdz*cdz;
    const float v23 = exp2f_fast(0.6666666865f * __log2f(0.5f * fabsf(det)));
-   const float q = 12.0f * v23 * __frcp_rn(l2);
+   const float q = __fdividef(12.0f * v23, l2);
    *inv = !pos;
    return pos ? q : -q;
 }
@@ -453,58 +623,8 @@ __device__ __forceinline__ void qacc_flush(QAcc &a, unsigned *hist, GmlxQualStat
       atomicAdd(&st->Hist[threadIdx.x], hist[threadIdx.x]);
 }
 
-/* ------------------------------------------------------------------------- */
-/* TMA bulk copies and mbarriers (inline PTX)                                 */
-/* ------------------------------------------------------------------------- */
-
-__device__ __forceinline__ unsigned smem_u32(const void *p)
-{
-   return (unsigned)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
-{
-   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
-{
-   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void tma_bulk_g2s(void *dst, const void *src, unsigned bytes,
-                                             unsigned long long *bar)
-{
-   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
-}
-
-/* non-blocking probe of the phase with the given parity */
-__device__ __forceinline__ int mbar_try_wait(unsigned long long *bar, unsigned parity)
-{
-   unsigned ok;
-   asm volatile("{\n\t.reg .pred p;\n\t"
-                "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                "selp.u32 %0, 1, 0, p;\n\t}"
-                : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
-   return (int)ok;
-}
-
-/* bounded wait: gives up after QK_SPIN polls (well under a second), so a
-   lost transfer ends the kernel with an error flag instead of hanging it */
-#define QK_SPIN (1 << 22)
-
-__device__ __forceinline__ int mbar_wait_bounded(unsigned long long *bar, unsigned parity)
-{
-   for(int i=0;i<QK_SPIN;i++)
-      if(mbar_try_wait(bar, parity))
-         return 1;
-   return 0;
-}
-
-#define QK_CHUNK  1024                     /* tets per stage: 16 KB */
-#define QK_STAGES 3
+#define QK_CHUNK  512                      /* tets per stage: 8 KB */
+#define QK_STAGES 4
 #define QK_SMEM   (QK_STAGES * QK_CHUNK * 16)
 
 /* The tetrahedron stream (16 bytes per tet, read once) is staged through
@@ -512,7 +632,7 @@ __device__ __forceinline__ int mbar_wait_bounded(unsigned long long *bar, unsign
    gathers (16 V bytes, L2 resident) are issued from registers, two tets per
    thread at a time.  Each warp handles 32 consecutive tets per pass, so its
    ballot is one word of the inverted-element bit flags. */
-__global__ void __launch_bounds__(MK_THREADS, 4)
+__global__ void __launch_bounds__(MK_THREADS, 5)
 tet_quality_tma_kernel(int nt, const int4 *__restrict__ tet, const float4 *__restrict__ crd,
                        float thr, float *__restrict__ qout, unsigned *__restrict__ flags,
                        GmlxQualStats *st, int *err)
@@ -565,9 +685,9 @@ tet_quality_tma_kernel(int nt, const int4 *__restrict__ tet, const float4 *__res
       const int n = min(QK_CHUNK, nt - start);
       const int4 *chunk = stage + s * QK_CHUNK;
 
-      /* 4 passes of 256 tets; a thread takes tets j and j + 512 together */
+      /* passes of 512 tets; a thread takes tets j and j + 256 together */
 #pragma unroll 1
-      for(int pass=0;pass<2;pass++)
+      for(int pass=0;pass<QK_CHUNK/(2*MK_THREADS);pass++)
       {
          const int j0 = pass * 2 * MK_THREADS + wid * 32 + lane;
          const int j1 = j0 + MK_THREADS;
@@ -661,11 +781,24 @@ extern "C" int gmd_mesh_point_fill(GmdCtx *ctx, const void *tet, int nrow, const
 }
 
 extern "C" int gmd_mesh_laplace(GmdCtx *ctx, int nrow, const unsigned *rowv, const long long *soff,
-                                const int *col, const void *in, void *out, float omega)
+                                const int *col, const void *in, void *out, float omega, int *err)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
-   laplace_sell_kernel<<<nblk(nrow, MK_THREADS), MK_THREADS, 0, st>>>(nrow, rowv, soff, col,
-      (const float4 *)in, (float4 *)out, omega);
+   static int attr_set = 0;
+   const int ntile = nrow / LT_ROWS;
+   long long cap = (long long)gmd_num_sms(ctx) * 3;
+   unsigned g = (unsigned)(ntile < cap ? ntile : cap);
+   if(ntile <= 0)
+      return 1;
+   if(!attr_set)
+   {
+      if(cudaFuncSetAttribute(laplace_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              LT_SMEM) != cudaSuccess)
+         return 0;
+      attr_set = 1;
+   }
+   laplace_tma_kernel<<<g, LT_ROWS, LT_SMEM, st>>>(ntile, rowv, soff, col, (const float4 *)in,
+                                                   (float4 *)out, omega, err);
    return cudaGetLastError() == cudaSuccess;
 }
 
@@ -682,7 +815,7 @@ extern "C" int gmd_mesh_quality(GmdCtx *ctx, int nt, const void *tet, const void
    static int attr_set = 0;
    cudaStream_t s = (cudaStream_t)gmd_stream(ctx);
    long long need = nblk(nt, QK_CHUNK);
-   long long cap = (long long)gmd_num_sms(ctx) * 4;
+   long long cap = (long long)gmd_num_sms(ctx) * 5;
    unsigned g = (unsigned)(need < cap ? need : cap);
    if(nt <= 0)
       return 1;

@@ -229,7 +229,7 @@ static int sweeps(GmlSct *gml, NatSct *n, GmlDatSct *ver, int ns, float omega)
    void *a = ver->GpuMem, *b = n->crd2;
    for(int s=0;s<ns;s++)
    {
-      if(!gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, a, b, omega))
+      if(!gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, a, b, omega, n->err))
          return 0;
       void *t = a; a = b; b = t;
    }
@@ -353,7 +353,7 @@ int GmlxSmoothQualityLoop(size_t GmlIdx, int nsweeps, float omega, double h, Gml
       gmd_mesh_stats_init(gml->dev, n->stats, nsweeps);
       for(int s=0;s<nsweeps;s++)
       {
-         gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, a, b, omega);
+         gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, a, b, omega, n->err);
          gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, b, det_threshold(h), NULL, n->flags,
                           n->stats + s, n->err);
          void *t = a; a = b; b = t;
