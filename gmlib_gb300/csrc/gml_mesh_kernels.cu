@@ -31,6 +31,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <float.h>
+#include <stdlib.h>
+#include <string.h>
 #include "gml_device.h"
 #include "gml_mesh.h"
 
@@ -239,20 +241,22 @@ __device__ __forceinline__ void tma_bulk_g2s(void *dst, const void *src, unsigne
                 :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
 
-/* non-blocking probe of the phase with the given parity */
+/* wait for the phase with the given parity; the thread is suspended in
+   hardware (no issue slots used) for at most about 20 us per call */
 __device__ __forceinline__ int mbar_try_wait(unsigned long long *bar, unsigned parity)
 {
    unsigned ok;
    asm volatile("{\n\t.reg .pred p;\n\t"
-                "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 20000;\n\t"
                 "selp.u32 %0, 1, 0, p;\n\t}"
                 : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
    return (int)ok;
 }
 
-/* bounded wait: gives up after QK_SPIN polls (well under a second), so a
-   lost transfer ends the kernel with an error flag instead of hanging it */
-#define QK_SPIN (1 << 22)
+/* bounded wait: gives up after QK_SPIN suspended tries (well under a
+   second in total), so a lost transfer ends the kernel with an error flag
+   instead of hanging it */
+#define QK_SPIN (1 << 14)
 
 __device__ __forceinline__ int mbar_wait_bounded(unsigned long long *bar, unsigned parity)
 {
@@ -784,8 +788,20 @@ extern "C" int gmd_mesh_laplace(GmdCtx *ctx, int nrow, const unsigned *rowv, con
                                 const int *col, const void *in, void *out, float omega, int *err)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
-   static int attr_set = 0;
+   static int attr_set = 0, variant = -1;
    const int ntile = nrow / LT_ROWS;
+   if(variant < 0)
+   {
+      /* GML_LAPLACE=sell selects the unstaged kernel (tuning and comparison) */
+      const char *e = getenv("GML_LAPLACE");
+      variant = (e && !strcmp(e, "sell")) ? 1 : 0;
+   }
+   if(variant == 1)
+   {
+      laplace_sell_kernel<<<nblk(nrow, MK_THREADS), MK_THREADS, 0, st>>>(nrow, rowv, soff, col,
+         (const float4 *)in, (float4 *)out, omega);
+      return cudaGetLastError() == cudaSuccess;
+   }
    long long cap = (long long)gmd_num_sms(ctx) * 3;
    unsigned g = (unsigned)(ntile < cap ? ntile : cap);
    if(ntile <= 0)
