@@ -26,6 +26,8 @@ struct GmdCtx
 {
    int            dev, nsm;
    cudaStream_t   stream;
+   cudaStream_t   side;          /* second stream for concurrent graph branches */
+   int            use_side;      /* 1: gmd_stream returns the side stream */
    char           err[512];
 };
 
@@ -146,6 +148,11 @@ extern "C" void gmd_stop(GmdCtx *ctx)
    cudaSetDevice(ctx->dev);
    cudaStreamSynchronize(ctx->stream);
    cudaStreamDestroy(ctx->stream);
+   if(ctx->side)
+   {
+      cudaStreamSynchronize(ctx->side);
+      cudaStreamDestroy(ctx->side);
+   }
    free(ctx);
 }
 
@@ -156,7 +163,43 @@ extern "C" int gmd_sync(GmdCtx *ctx)
    return ok(ctx, cudaStreamSynchronize(ctx->stream), "stream synchronize");
 }
 
-extern "C" void *gmd_stream(GmdCtx *ctx) { return ctx ? (void *)ctx->stream : NULL; }
+extern "C" void *gmd_stream(GmdCtx *ctx)
+{
+   if(!ctx)
+      return NULL;
+   return ctx->use_side ? (void *)ctx->side : (void *)ctx->stream;
+}
+
+/* route subsequent work of the instance to its side stream (1) or back to
+   the main stream (0) */
+extern "C" int gmd_use_side(GmdCtx *ctx, int on)
+{
+   if(!ctx)
+      return 0;
+   if(on && !ctx->side
+   && cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess)
+      return 0;
+   ctx->use_side = on ? 1 : 0;
+   return 1;
+}
+
+/* event without timing, for ordering streams (also inside graph capture) */
+extern "C" void *gmd_event_new_sync(void)
+{
+   cudaEvent_t e;
+   if(cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+      return NULL;
+   return (void *)e;
+}
+
+/* the current stream of the instance waits for an event */
+extern "C" int gmd_stream_wait(GmdCtx *ctx, void *evt)
+{
+   if(!ctx || !evt)
+      return 0;
+   return ok(ctx, cudaStreamWaitEvent((cudaStream_t)gmd_stream(ctx), (cudaEvent_t)evt, 0),
+             "stream wait");
+}
 extern "C" const char *gmd_last_error(GmdCtx *ctx) { return ctx ? ctx->err : ""; }
 extern "C" int gmd_num_sms(GmdCtx *ctx) { return ctx ? ctx->nsm : 1; }
 
@@ -262,7 +305,7 @@ extern "C" int gmd_event_record(GmdCtx *ctx, void *evt)
 {
    if(!ctx || !evt)
       return 0;
-   return ok(ctx, cudaEventRecord((cudaEvent_t)evt, ctx->stream), "event record");
+   return ok(ctx, cudaEventRecord((cudaEvent_t)evt, (cudaStream_t)gmd_stream(ctx)), "event record");
 }
 
 extern "C" int gmd_event_wait(void *evt)

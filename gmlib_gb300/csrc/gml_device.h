@@ -52,6 +52,9 @@ int      gmd_event_record(GmdCtx *ctx, void *evt);
 int      gmd_event_wait(void *evt);
 double   gmd_event_elapsed_s(void *beg, void *end);    /* synchronises on end */
 int      gmd_capturing(GmdCtx *ctx);                   /* stream under graph capture */
+int      gmd_use_side(GmdCtx *ctx, int on);            /* work goes to the side stream */
+void    *gmd_event_new_sync(void);                     /* event without timing */
+int      gmd_stream_wait(GmdCtx *ctx, void *evt);      /* current stream waits for evt */
 
 /* NVRTC + modules ----------------------------------------------------------- */
 /* Compile a generated CUDA source to an sm_103a cubin.  Returns 1 on success;

@@ -349,6 +349,82 @@ laplace_sell_kernel(int nrow, const unsigned *__restrict__ rowv, const long long
                         p.z + omega * (sz * inv - p.z), 0.f);
 }
 
+/* The sweep as a persistent kernel: warp w handles slices w, w + W, ...
+   and, before working on a slice, asks the TMA unit to prefetch the column
+   block of its next slice into L2 (cp.async.bulk.prefetch.L2), so the
+   column loads of the next slice hit L2 instead of HBM.  Inside a row the
+   column loads of entries k+4..k+7 are issued before the coordinate
+   gathers of entries k..k+3, keeping about eight loads in flight per
+   thread. */
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes)
+{
+   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
+}
+
+__global__ void __launch_bounds__(MK_THREADS)
+laplace_pf_kernel(int nslice, const unsigned *__restrict__ rowv, const long long *__restrict__ soff,
+                  const int *__restrict__ col, const float4 *__restrict__ in,
+                  float4 *__restrict__ out, float omega)
+{
+   const int lane = threadIdx.x & 31;
+   const int w0 = (blockIdx.x * MK_THREADS + threadIdx.x) >> 5;
+   const int nw = (gridDim.x * MK_THREADS) >> 5;
+
+   if(lane == 0 && w0 < nslice)
+   {
+      const long long c0 = __ldg(&soff[w0]), c1 = __ldg(&soff[w0 + 1]);
+      if(c1 > c0)
+         prefetch_l2(col + c0 * 32, (unsigned)((c1 - c0) * 128));
+   }
+
+   for(int sl=w0; sl<nslice; sl+=nw)
+   {
+      const int nx = sl + nw;
+      if(lane == 0 && nx < nslice)
+      {
+         const long long c0 = __ldg(&soff[nx]), c1 = __ldg(&soff[nx + 1]);
+         if(c1 > c0)
+            prefetch_l2(col + c0 * 32, (unsigned)((c1 - c0) * 128));
+      }
+      const unsigned pk = __ldg(&rowv[ sl * 32 + lane ]);
+      if(pk == ROW_NONE)
+         continue;
+      const int v = (int)(pk & ROW_MASK), d = (int)(pk >> ROW_SHIFT);
+      const float4 p = __ldg(&in[v]);
+      if(d == 0)
+      {
+         out[v] = p;
+         continue;
+      }
+      const int *cp = col + __ldg(&soff[sl]) * 32 + lane;
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      int c[4];
+#pragma unroll
+      for(int u=0;u<4;u++)
+         c[u] = u < d ? __ldg(cp + u * 32) : 0;
+      for(int k=0;k<d;k+=4)
+      {
+         int nc[4];
+#pragma unroll
+         for(int u=0;u<4;u++)
+            nc[u] = k + 4 + u < d ? __ldg(cp + (size_t)(k + 4 + u) * 32) : 0;
+#pragma unroll
+         for(int u=0;u<4;u++)
+            if(k + u < d)
+            {
+               const float4 q = __ldg(&in[ c[u] ]);
+               sx += q.x; sy += q.y; sz += q.z;
+            }
+#pragma unroll
+         for(int u=0;u<4;u++)
+            c[u] = nc[u];
+      }
+      const float inv = 1.0f / (float)d;
+      out[v] = make_float4(p.x + omega * (sx * inv - p.x), p.y + omega * (sy * inv - p.y),
+                           p.z + omega * (sz * inv - p.z), 0.f);
+   }
+}
+
 /* The same sweep with the column block of each 256-row tile (8 slices,
    contiguous in the SELL arrays) staged into shared memory by a TMA bulk
    copy issued one tile ahead, so that the column stream never sits on the
@@ -792,9 +868,18 @@ extern "C" int gmd_mesh_laplace(GmdCtx *ctx, int nrow, const unsigned *rowv, con
    const int ntile = nrow / LT_ROWS;
    if(variant < 0)
    {
-      /* GML_LAPLACE=sell selects the unstaged kernel (tuning and comparison) */
+      /* GML_LAPLACE=sell|tma|pf selects the sweep kernel (default pf) */
       const char *e = getenv("GML_LAPLACE");
-      variant = (e && !strcmp(e, "sell")) ? 1 : 0;
+      variant = !e ? 2 : !strcmp(e, "sell") ? 1 : !strcmp(e, "tma") ? 0 : 2;
+   }
+   if(variant == 2)
+   {
+      const int nslice = nrow / 32;
+      long long need = nblk(nslice, MK_THREADS / 32), cap2 = (long long)gmd_num_sms(ctx) * 6;
+      unsigned g2 = (unsigned)(need < cap2 ? need : cap2);
+      laplace_pf_kernel<<<g2, MK_THREADS, 0, st>>>(nslice, rowv, soff, col, (const float4 *)in,
+                                                   (float4 *)out, omega);
+      return cudaGetLastError() == cudaSuccess;
    }
    if(variant == 1)
    {

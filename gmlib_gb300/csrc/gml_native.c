@@ -11,6 +11,8 @@
 #include "gmlib3_gb300.h"
 #include "gml_mesh.h"
 
+#define GML_MAXSTATS 64
+
 typedef struct
 {
    int         nv, nt, fix, ready;
@@ -29,10 +31,10 @@ typedef struct
    float       gomega;
    double      gh;
    void        *gver, *gtet;          /* buffers the graph was captured on */
+   void        *evL[GML_MAXSTATS + 1], *evQ[GML_MAXSTATS + 1];   /* graph ordering */
    int         NmbLoopKrn, NmbSweepKrn, NmbQalKrn;
 }NatSct;
 
-#define GML_MAXSTATS 64
 
 static NatSct *nat(GmlSct *gml)
 {
@@ -52,6 +54,11 @@ static void free_state(GmlSct *gml, NatSct *n)
    gmd_free(gml->dev, n->crd2);
    gmd_free(gml->dev, n->flags); gmd_free(gml->dev, n->stats);
    gmd_graph_free(n->graph);
+   for(int e=0;e<=GML_MAXSTATS;e++)
+   {
+      gmd_event_free(n->evL[e]);
+      gmd_event_free(n->evQ[e]);
+   }
    memset(n, 0, sizeof(NatSct));
 }
 
@@ -348,18 +355,42 @@ int GmlxSmoothQualityLoop(size_t GmlIdx, int nsweeps, float omega, double h, Gml
       void *a = ver->GpuMem, *b = n->crd2;
       gmd_graph_free(n->graph);
       n->graph = NULL;
+      /* Sweep s+1 and the quality of sweep s read the same coordinates and
+         are independent: the graph runs them on two streams.  Sweep s+2
+         overwrites the buffer that quality s reads (ping-pong), so it waits
+         for it.  x_s lives in a when s is even, in b when s is odd. */
+      if(!n->evL[0])
+         for(int e=0;e<=GML_MAXSTATS;e++)
+         {
+            n->evL[e] = gmd_event_new_sync();
+            n->evQ[e] = gmd_event_new_sync();
+         }
       if(!gmd_graph_begin(gml->dev))
          return 0;
       gmd_mesh_stats_init(gml->dev, n->stats, nsweeps);
-      for(int s=0;s<nsweeps;s++)
+      gmd_event_record(gml->dev, n->evL[0]);
+      gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, a, b, omega, n->err);
+      gmd_event_record(gml->dev, n->evL[1]);
+      for(int s=1;s<=nsweeps;s++)
       {
-         gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, a, b, omega, n->err);
-         gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, b, det_threshold(h), NULL, n->flags,
-                          n->stats + s, n->err);
-         void *t = a; a = b; b = t;
+         void *xs = (s & 1) ? b : a, *xn = (s & 1) ? a : b;
+         gmd_use_side(gml->dev, 1);
+         gmd_stream_wait(gml->dev, n->evL[s]);
+         gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, xs, det_threshold(h), NULL, n->flags,
+                          n->stats + s - 1, n->err);
+         gmd_event_record(gml->dev, n->evQ[s]);
+         gmd_use_side(gml->dev, 0);
+         if(s < nsweeps)
+         {
+            if(s >= 2)
+               gmd_stream_wait(gml->dev, n->evQ[s-1]);
+            gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, xs, xn, omega, n->err);
+            gmd_event_record(gml->dev, n->evL[s+1]);
+         }
       }
-      if(a != ver->GpuMem)
-         gmd_d2d_async(gml->dev, ver->GpuMem, a, (size_t)n->nv * 16);
+      gmd_stream_wait(gml->dev, n->evQ[nsweeps]);
+      if(nsweeps & 1)
+         gmd_d2d_async(gml->dev, ver->GpuMem, b, (size_t)n->nv * 16);
       if(!gmd_graph_end(gml->dev, &n->graph))
          return 0;
       n->gsweeps = nsweeps;
