@@ -361,6 +361,7 @@ __device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes)
    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
 }
 
+template<int U>
 __global__ void __launch_bounds__(MK_THREADS)
 laplace_pf_kernel(int nslice, const unsigned *__restrict__ rowv, const long long *__restrict__ soff,
                   const int *__restrict__ col, const float4 *__restrict__ in,
@@ -398,25 +399,25 @@ laplace_pf_kernel(int nslice, const unsigned *__restrict__ rowv, const long long
       }
       const int *cp = col + __ldg(&soff[sl]) * 32 + lane;
       float sx = 0.f, sy = 0.f, sz = 0.f;
-      int c[4];
+      int c[U];
 #pragma unroll
-      for(int u=0;u<4;u++)
+      for(int u=0;u<U;u++)
          c[u] = u < d ? __ldg(cp + u * 32) : 0;
-      for(int k=0;k<d;k+=4)
+      for(int k=0;k<d;k+=U)
       {
-         int nc[4];
+         int nc[U];
 #pragma unroll
-         for(int u=0;u<4;u++)
-            nc[u] = k + 4 + u < d ? __ldg(cp + (size_t)(k + 4 + u) * 32) : 0;
+         for(int u=0;u<U;u++)
+            nc[u] = k + U + u < d ? __ldg(cp + (size_t)(k + U + u) * 32) : 0;
 #pragma unroll
-         for(int u=0;u<4;u++)
+         for(int u=0;u<U;u++)
             if(k + u < d)
             {
                const float4 q = __ldg(&in[ c[u] ]);
                sx += q.x; sy += q.y; sz += q.z;
             }
 #pragma unroll
-         for(int u=0;u<4;u++)
+         for(int u=0;u<U;u++)
             c[u] = nc[u];
       }
       const float inv = 1.0f / (float)d;
@@ -582,6 +583,20 @@ __global__ void stats_init_kernel(GmlxQualStats *st, int n)
    rounding error), *f64 = 1 when the FP64 determinant was used.
    q = 12 (|det|/2)^(2/3) / l2 is evaluated with the special-function unit
    (log2/exp2, about 2^-22 relative error) and a fast reciprocal. */
+/* FP64 determinant of the FP32 coordinates (rare path, kept out of line so
+   that it costs nothing to the common path); returns det > 0 */
+__device__ __noinline__ int det64_positive(const float4 a, const float4 b, const float4 c,
+                                           const float4 d, float *det)
+{
+   const double Ax = a.x, Ay = a.y, Az = a.z;
+   const double bx = b.x - Ax, by = b.y - Ay, bz = b.z - Az;
+   const double cx = c.x - Ax, cy = c.y - Ay, cz = c.z - Az;
+   const double dx = d.x - Ax, dy = d.y - Ay, dz = d.z - Az;
+   const double dd = bx * (cy * dz - cz * dy) + by * (cz * dx - cx * dz) + bz * (cx * dy - cy * dx);
+   *det = (float)dd;
+   return dd > 0.;
+}
+
 __device__ __forceinline__ float tet_mean_ratio(const int4 e, const float4 *__restrict__ crd,
                                                 float thr, int *inv, int *f64)
 {
@@ -590,31 +605,25 @@ __device__ __forceinline__ float tet_mean_ratio(const int4 e, const float4 *__re
    const float abx = b.x - a.x, aby = b.y - a.y, abz = b.z - a.z;
    const float acx = c.x - a.x, acy = c.y - a.y, acz = c.z - a.z;
    const float adx = d.x - a.x, ady = d.y - a.y, adz = d.z - a.z;
-   float det = abx * (acy * adz - acz * ady) + aby * (acz * adx - acx * adz)
-             + abz * (acx * ady - acy * adx);
-   int pos = det > 0.f;
-   /* |det| error bound: 16 eps32 times a product that dominates the sum of
-      the absolute values of the six products of the expansion */
-   const float bnd = (fabsf(abx) + fabsf(aby) + fabsf(abz)) * (fabsf(acx) + fabsf(acy) + fabsf(acz))
-                   * (fabsf(adx) + fabsf(ady) + fabsf(adz));
-   *f64 = 0;
-   if(fabsf(det) < fmaxf(thr, 9.5367431640625e-07f * bnd))
-   {
-      const double Ax = a.x, Ay = a.y, Az = a.z;
-      const double bx = b.x - Ax, by = b.y - Ay, bz = b.z - Az;
-      const double cx = c.x - Ax, cy = c.y - Ay, cz = c.z - Az;
-      const double dx = d.x - Ax, dy = d.y - Ay, dz = d.z - Az;
-      const double dd = bx * (cy * dz - cz * dy) + by * (cz * dx - cx * dz) + bz * (cx * dy - cy * dx);
-      det = (float)dd;
-      pos = dd > 0.;
-      *f64 = 1;
-   }
    const float bcx = acx - abx, bcy = acy - aby, bcz = acz - abz;
    const float bdx = adx - abx, bdy = ady - aby, bdz = adz - abz;
    const float cdx = adx - acx, cdy = ady - acy, cdz = adz - acz;
    const float l2 = abx*abx + aby*aby + abz*abz + acx*acx + acy*acy + acz*acz
                   + adx*adx + ady*ady + adz*adz + bcx*bcx + bcy*bcy + bcz*bcz
                   + bdx*bdx + bdy*bdy + bdz*bdz + cdx*cdx + cdy*cdy + cdz*cdz;
+   float det = abx * (acy * adz - acz * ady) + aby * (acz * adx - acx * adz)
+             + abz * (acx * ady - acy * adx);
+   int pos = det > 0.f;
+   /* The FP32 determinant is off by at most about 7 eps32 times the sum of
+      the absolute values of its six products, a sum bounded by
+      (|ab|_1 |ac|_1 |ad|_1) <= l2^(3/2); below 16 eps32 l2^(3/2) (1% margin
+      for rsqrt) the sign is taken from the FP64 determinant. */
+   *f64 = 0;
+   if(fabsf(det) < fmaxf(thr, 9.7e-07f * l2 * l2 * rsqrtf(l2)))
+   {
+      pos = det64_positive(a, b, c, d, &det);
+      *f64 = 1;
+   }
    const float v23 = exp2f_fast(0.6666666865f * __log2f(0.5f * fabsf(det)));
    const float q = __fdividef(12.0f * v23, l2);
    *inv = !pos;
@@ -777,13 +786,22 @@ tet_quality_tma_kernel(int nt, const int4 *__restrict__ tet, const float4 *__res
          if(j1 < n) q1 = tet_mean_ratio(chunk[j1], crd, thr, &inv1, &f1);
          if(j0 < n)
          {
-            qacc_add(a, q0, start + j0, f0);
+            if(q0 < a.mn) { a.mn = q0; a.mi = start + j0; }
+            if(q0 > a.mx) { a.mx = q0; a.xi = start + j0; }
             if(qout) qout[start + j0] = q0;
          }
          if(j1 < n)
          {
-            qacc_add(a, q1, start + j1, f1);
+            if(q1 < a.mn) { a.mn = q1; a.mi = start + j1; }
+            if(q1 > a.mx) { a.mx = q1; a.xi = start + j1; }
             if(qout) qout[start + j1] = q1;
+         }
+         {
+            /* one TwoSum per pair (invalid tets contribute 0) */
+            const float pq = q0 + q1, tt = a.s + pq, bp = tt - a.s;
+            a.c += (a.s - (tt - bp)) + (pq - bp);
+            a.s = tt;
+            a.nf64 += f0 + f1;
          }
          hist_add_warp(hist, q0, j0 < n, lane);
          hist_add_warp(hist, q1, j1 < n, lane);
@@ -868,17 +886,21 @@ extern "C" int gmd_mesh_laplace(GmdCtx *ctx, int nrow, const unsigned *rowv, con
    const int ntile = nrow / LT_ROWS;
    if(variant < 0)
    {
-      /* GML_LAPLACE=sell|tma|pf selects the sweep kernel (default pf) */
+      /* GML_LAPLACE = sell, tma, pf or pf8 selects the sweep kernel (default pf8) */
       const char *e = getenv("GML_LAPLACE");
-      variant = !e ? 2 : !strcmp(e, "sell") ? 1 : !strcmp(e, "tma") ? 0 : 2;
+      variant = !e ? 3 : !strcmp(e, "sell") ? 1 : !strcmp(e, "tma") ? 0 : !strcmp(e, "pf") ? 2 : 3;
    }
-   if(variant == 2)
+   if(variant >= 2)
    {
       const int nslice = nrow / 32;
       long long need = nblk(nslice, MK_THREADS / 32), cap2 = (long long)gmd_num_sms(ctx) * 6;
       unsigned g2 = (unsigned)(need < cap2 ? need : cap2);
-      laplace_pf_kernel<<<g2, MK_THREADS, 0, st>>>(nslice, rowv, soff, col, (const float4 *)in,
-                                                   (float4 *)out, omega);
+      if(variant == 2)
+         laplace_pf_kernel<4><<<g2, MK_THREADS, 0, st>>>(nslice, rowv, soff, col, (const float4 *)in,
+                                                         (float4 *)out, omega);
+      else
+         laplace_pf_kernel<8><<<g2, MK_THREADS, 0, st>>>(nslice, rowv, soff, col, (const float4 *)in,
+                                                         (float4 *)out, omega);
       return cudaGetLastError() == cudaSuccess;
    }
    if(variant == 1)
