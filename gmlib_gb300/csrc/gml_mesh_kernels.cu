@@ -556,6 +556,21 @@ __device__ __forceinline__ unsigned mk_fkey(float f)
    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
+/* log2(x) and 1/sqrt(x) on the special-function unit */
+__device__ __forceinline__ float log2f_fast(float x)
+{
+   float y;
+   asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+   return y;
+}
+
+__device__ __forceinline__ float rsqrtf_fast(float x)
+{
+   float y;
+   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+   return y;
+}
+
 /* 2^x on the special-function unit (ex2.approx.ftz.f32) */
 __device__ __forceinline__ float exp2f_fast(float x)
 {
@@ -619,12 +634,12 @@ __device__ __forceinline__ float tet_mean_ratio(const int4 e, const float4 *__re
       (|ab|_1 |ac|_1 |ad|_1) <= l2^(3/2); below 16 eps32 l2^(3/2) (1% margin
       for rsqrt) the sign is taken from the FP64 determinant. */
    *f64 = 0;
-   if(fabsf(det) < fmaxf(thr, 9.7e-07f * l2 * l2 * rsqrtf(l2)))
+   if(fabsf(det) < fmaxf(thr, 9.7e-07f * l2 * l2 * rsqrtf_fast(l2)))
    {
       pos = det64_positive(a, b, c, d, &det);
       *f64 = 1;
    }
-   const float v23 = exp2f_fast(0.6666666865f * __log2f(0.5f * fabsf(det)));
+   const float v23 = exp2f_fast(0.6666666865f * log2f_fast(0.5f * fabsf(det)));
    const float q = __fdividef(12.0f * v23, l2);
    *inv = !pos;
    return pos ? q : -q;
@@ -721,6 +736,51 @@ __device__ __forceinline__ void qacc_flush(QAcc &a, unsigned *hist, GmlxQualStat
    gathers (16 V bytes, L2 resident) are issued from registers, two tets per
    thread at a time.  Each warp handles 32 consecutive tets per pass, so its
    ballot is one word of the inverted-element bit flags. */
+/* one pass over 512 tets of a staged chunk: a thread takes tets j and
+   j + 256; FULL (every tet valid) removes all validity tests, WQ writes the
+   per-tet quality */
+template<bool FULL, bool WQ>
+__device__ __forceinline__ void quality_pass(const int4 *chunk, int n, int start, int pass,
+                                             const float4 *__restrict__ crd, float thr,
+                                             float *__restrict__ qout, unsigned *__restrict__ flags,
+                                             QAcc &a, unsigned *hist, int lane, int wid)
+{
+   const int j0 = pass * 2 * MK_THREADS + wid * 32 + lane, j1 = j0 + MK_THREADS;
+   const bool v0 = FULL || j0 < n, v1 = FULL || j1 < n;
+   int inv0 = 0, inv1 = 0, f0 = 0, f1 = 0;
+   float q0 = 0.f, q1 = 0.f;
+   if(v0) q0 = tet_mean_ratio(chunk[j0], crd, thr, &inv0, &f0);
+   if(v1) q1 = tet_mean_ratio(chunk[j1], crd, thr, &inv1, &f1);
+   if(v0 && q0 < a.mn) { a.mn = q0; a.mi = start + j0; }
+   if(v0 && q0 > a.mx) { a.mx = q0; a.xi = start + j0; }
+   if(v1 && q1 < a.mn) { a.mn = q1; a.mi = start + j1; }
+   if(v1 && q1 > a.mx) { a.mx = q1; a.xi = start + j1; }
+   if(WQ)
+   {
+      if(v0) qout[start + j0] = q0;
+      if(v1) qout[start + j1] = q1;
+   }
+   {
+      /* one TwoSum per pair (invalid tets contribute 0) */
+      const float pq = q0 + q1, tt = a.s + pq, bp = tt - a.s;
+      a.c += (a.s - (tt - bp)) + (pq - bp);
+      a.s = tt;
+      a.nf64 += f0 + f1;
+   }
+   hist_add_warp(hist, q0, v0, lane);
+   hist_add_warp(hist, q1, v1, lane);
+   const unsigned w0 = __ballot_sync(0xffffffffu, inv0);
+   const unsigned w1 = __ballot_sync(0xffffffffu, inv1);
+   if(lane == 0)
+   {
+      const int b0 = pass * 2 * MK_THREADS + wid * 32, b1 = b0 + MK_THREADS;
+      a.ninv += __popc(w0) + __popc(w1);
+      if(FULL || b0 < n) flags[ (start + b0) >> 5 ] = w0;
+      if(FULL || b1 < n) flags[ (start + b1) >> 5 ] = w1;
+   }
+}
+
+template<bool WQ>
 __global__ void __launch_bounds__(MK_THREADS, 5)
 tet_quality_tma_kernel(int nt, const int4 *__restrict__ tet, const float4 *__restrict__ crd,
                        float thr, float *__restrict__ qout, unsigned *__restrict__ flags,
@@ -774,46 +834,18 @@ tet_quality_tma_kernel(int nt, const int4 *__restrict__ tet, const float4 *__res
       const int n = min(QK_CHUNK, nt - start);
       const int4 *chunk = stage + s * QK_CHUNK;
 
-      /* passes of 512 tets; a thread takes tets j and j + 256 together */
-#pragma unroll 1
-      for(int pass=0;pass<QK_CHUNK/(2*MK_THREADS);pass++)
+      /* passes of 512 tets; only the last chunk can be partial */
+      if(n == QK_CHUNK)
       {
-         const int j0 = pass * 2 * MK_THREADS + wid * 32 + lane;
-         const int j1 = j0 + MK_THREADS;
-         int inv0 = 0, inv1 = 0, f0 = 0, f1 = 0;
-         float q0 = 0.f, q1 = 0.f;
-         if(j0 < n) q0 = tet_mean_ratio(chunk[j0], crd, thr, &inv0, &f0);
-         if(j1 < n) q1 = tet_mean_ratio(chunk[j1], crd, thr, &inv1, &f1);
-         if(j0 < n)
-         {
-            if(q0 < a.mn) { a.mn = q0; a.mi = start + j0; }
-            if(q0 > a.mx) { a.mx = q0; a.xi = start + j0; }
-            if(qout) qout[start + j0] = q0;
-         }
-         if(j1 < n)
-         {
-            if(q1 < a.mn) { a.mn = q1; a.mi = start + j1; }
-            if(q1 > a.mx) { a.mx = q1; a.xi = start + j1; }
-            if(qout) qout[start + j1] = q1;
-         }
-         {
-            /* one TwoSum per pair (invalid tets contribute 0) */
-            const float pq = q0 + q1, tt = a.s + pq, bp = tt - a.s;
-            a.c += (a.s - (tt - bp)) + (pq - bp);
-            a.s = tt;
-            a.nf64 += f0 + f1;
-         }
-         hist_add_warp(hist, q0, j0 < n, lane);
-         hist_add_warp(hist, q1, j1 < n, lane);
-         const unsigned w0 = __ballot_sync(0xffffffffu, inv0);
-         const unsigned w1 = __ballot_sync(0xffffffffu, inv1);
-         if(lane == 0)
-         {
-            const int b0 = pass * 2 * MK_THREADS + wid * 32, b1 = b0 + MK_THREADS;
-            a.ninv += __popc(w0) + __popc(w1);
-            if(flags && b0 < n) flags[ (start + b0) >> 5 ] = w0;
-            if(flags && b1 < n) flags[ (start + b1) >> 5 ] = w1;
-         }
+#pragma unroll
+         for(int pass=0;pass<QK_CHUNK/(2*MK_THREADS);pass++)
+            quality_pass<true, WQ>(chunk, n, start, pass, crd, thr, qout, flags, a, hist, lane, wid);
+      }
+      else
+      {
+#pragma unroll 1
+         for(int pass=0;pass<QK_CHUNK/(2*MK_THREADS);pass++)
+            quality_pass<false, WQ>(chunk, n, start, pass, crd, thr, qout, flags, a, hist, lane, wid);
       }
 
       /* every thread is done with stage s: refill it */
@@ -944,12 +976,20 @@ extern "C" int gmd_mesh_quality(GmdCtx *ctx, int nt, const void *tet, const void
       return 1;
    if(!attr_set)
    {
-      if(cudaFuncSetAttribute(tet_quality_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      if(cudaFuncSetAttribute(tet_quality_tma_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              QK_SMEM) != cudaSuccess
+      || cudaFuncSetAttribute(tet_quality_tma_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               QK_SMEM) != cudaSuccess)
          return 0;
       attr_set = 1;
    }
-   tet_quality_tma_kernel<<<g, MK_THREADS, QK_SMEM, s>>>(nt, (const int4 *)tet, (const float4 *)crd,
-                                                         thr, qout, flags, st, err);
+   if(!flags)
+      return 0;
+   if(qout)
+      tet_quality_tma_kernel<true><<<g, MK_THREADS, QK_SMEM, s>>>(nt, (const int4 *)tet,
+         (const float4 *)crd, thr, qout, flags, st, err);
+   else
+      tet_quality_tma_kernel<false><<<g, MK_THREADS, QK_SMEM, s>>>(nt, (const int4 *)tet,
+         (const float4 *)crd, thr, qout, flags, st, err);
    return cudaGetLastError() == cudaSuccess;
 }
