@@ -12,7 +12,8 @@ import os
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libgmlib3.so")
+# GML_LIB overrides the library path (tuning builds made with build(out=...))
+LIB_PATH = os.environ.get("GML_LIB") or os.path.join(_HERE, "libgmlib3.so")
 
 # enums of gmlib3.h
 GmlVertices, GmlEdges, GmlTriangles, GmlQuadrilaterals, GmlTetrahedra, \

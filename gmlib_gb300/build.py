@@ -81,8 +81,13 @@ def _run(cmd):
     return r.stdout
 
 
-def build(force=False, verbose=False):
-    os.makedirs(BUILD, exist_ok=True)
+def build(force=False, verbose=False, defines=(), out=None, objdir=None):
+    """Compile and link the library.  defines: extra -D macros for the CUDA
+    sources (tuning variants); out / objdir: alternate library path and
+    object directory for such variants."""
+    lib = out or LIB
+    bdir = objdir or BUILD
+    os.makedirs(bdir, exist_ok=True)
     emb = _embed()
     hdrs = _headers()
     jobs, objs = [], []
@@ -90,15 +95,15 @@ def build(force=False, verbose=False):
               "-I" + INCLUDE, "-I" + CSRC, "-I" + os.path.join(CUDA_HOME, "include")]
     for f in C_SOURCES + [emb]:
         src = f if os.path.isabs(f) else os.path.join(CSRC, f)
-        obj = os.path.join(BUILD, os.path.basename(f) + ".o")
+        obj = os.path.join(bdir, os.path.basename(f) + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
             jobs.append(["gcc"] + cflags + ["-c", src, "-o", obj])
     nvflags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                      "-I" + INCLUDE, "-I" + CSRC]
+                      "-I" + INCLUDE, "-I" + CSRC] + ["-D" + d for d in defines]
     for f in CU_SOURCES:
         src = os.path.join(CSRC, f)
-        obj = os.path.join(BUILD, f + ".o")
+        obj = os.path.join(bdir, f + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
             jobs.append([NVCC] + nvflags + ["-c", src, "-o", obj])
@@ -109,15 +114,14 @@ def build(force=False, verbose=False):
             for o in outs:
                 if o.strip():
                     print(o)
-    if jobs or force or not os.path.exists(LIB):
+    if jobs or force or not os.path.exists(lib):
         libdirs = _cuda_libdirs()
-        link = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs
+        link = [NVCC] + ARCH + ["-shared", "-o", lib] + objs
         for d in libdirs:
             link += ["-L" + d, "-Xlinker", "-rpath=" + d]
         link += ["-cudart", "static", "-lnvrtc", "-lpthread", "-ldl", "-lrt", "-lm"]
         _run(link)
-    return LIB
-
+    return lib
 
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))

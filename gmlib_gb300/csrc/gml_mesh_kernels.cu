@@ -727,8 +727,15 @@ __device__ __forceinline__ void qacc_flush(QAcc &a, unsigned *hist, GmlxQualStat
       atomicAdd(&st->Hist[threadIdx.x], hist[threadIdx.x]);
 }
 
+#ifndef QK_CHUNK
 #define QK_CHUNK  512                      /* tets per stage: 8 KB */
+#endif
+#ifndef QK_STAGES
 #define QK_STAGES 4
+#endif
+#ifndef QK_BLOCKS
+#define QK_BLOCKS 5                        /* resident blocks per SM */
+#endif
 #define QK_SMEM   (QK_STAGES * QK_CHUNK * 16)
 
 /* The tetrahedron stream (16 bytes per tet, read once) is staged through
@@ -781,7 +788,7 @@ __device__ __forceinline__ void quality_pass(const int4 *chunk, int n, int start
 }
 
 template<bool WQ>
-__global__ void __launch_bounds__(MK_THREADS, 5)
+__global__ void __launch_bounds__(MK_THREADS, QK_BLOCKS)
 tet_quality_tma_kernel(int nt, const int4 *__restrict__ tet, const float4 *__restrict__ crd,
                        float thr, float *__restrict__ qout, unsigned *__restrict__ flags,
                        GmlxQualStats *st, int *err)
@@ -970,7 +977,7 @@ extern "C" int gmd_mesh_quality(GmdCtx *ctx, int nt, const void *tet, const void
    static int attr_set = 0;
    cudaStream_t s = (cudaStream_t)gmd_stream(ctx);
    long long need = nblk(nt, QK_CHUNK);
-   long long cap = (long long)gmd_num_sms(ctx) * 5;
+   long long cap = (long long)gmd_num_sms(ctx) * QK_BLOCKS;
    unsigned g = (unsigned)(need < cap ? need : cap);
    if(nt <= 0)
       return 1;
