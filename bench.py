@@ -312,8 +312,8 @@ def run_gpu(args, dist):
     G.lib.GmlxEventRecord(g, e1)
     t_qual = G.lib.GmlxEventElapsed(e0, e1) / reps
     peak, peak_src = peak_hbm()
-    kern = [("laplace_sell_kernel", sweep_b.value, t_sweep),
-            ("tet_quality_kernel", qual_b.value, t_qual)]
+    kern = [("laplace_pf_kernel", sweep_b.value, t_sweep),
+            ("tet_quality_tma_kernel", qual_b.value, t_qual)]
     kern.sort(key=lambda k: -k[2])
     name, kb, kt = kern[0]
     achieved = kb / kt / 1e9

@@ -731,10 +731,10 @@ __device__ __forceinline__ void qacc_flush(QAcc &a, unsigned *hist, GmlxQualStat
 #define QK_CHUNK  512                      /* tets per stage: 8 KB */
 #endif
 #ifndef QK_STAGES
-#define QK_STAGES 4
+#define QK_STAGES 3
 #endif
 #ifndef QK_BLOCKS
-#define QK_BLOCKS 5                        /* resident blocks per SM */
+#define QK_BLOCKS 6                        /* resident blocks per SM */
 #endif
 #define QK_SMEM   (QK_STAGES * QK_CHUNK * 16)
 
