@@ -124,6 +124,7 @@ SIGNATURES.update({
     "GmlxEventRecord": (_i, [_s, _p]),
     "GmlxEventElapsed": (_d, [_p, _p]),
     "GmlxEventDestroy": (None, [_p]),
+    "GmlxReduceNoAlloc": (_i, [_p, _s, _i, _dp, _p]),
 })
 
 

@@ -27,8 +27,12 @@
 #include <cuda_runtime.h>
 #include <float.h>
 #include <stdint.h>
+#include <stdarg.h>
+#include <stdio.h>
 #include <string.h>
+#include <mutex>
 #include "gml_device.h"
+#include "gmlib3_gb300.h"
 
 #define RED_THREADS 512
 #define RED_MAXBLK  1024
@@ -310,5 +314,108 @@ extern "C" int gmd_minmax_arg_f32(GmdCtx *ctx, const float *in, int n,
       if(vmax) *vmax = fmx;
       if(imax) *imax = (int)(host[1] & 0xffffffffu);
    }
+   return 1;
+}
+
+/* ------------------------------------------------------------------------- */
+/* GmlxReduceNoAlloc: the reduction above with its scratch in static device   */
+/* memory, for callers that cannot allocate                                   */
+/* ------------------------------------------------------------------------- */
+
+/* [0] ticket, [1] result, [2, 2 + RED_MAXBLK) per-block partials.  Static
+   device storage is zero when the module loads, so the ticket starts at
+   zero; every completed launch re-arms it to zero in its last block.  The
+   array exists once per device: calls in flight at the same time on one
+   device (two streams, or two host threads) share it and race. */
+static __device__ __align__(256) unsigned long long gml_noalloc_scratch[2 + RED_MAXBLK];
+
+#define NOALLOC_MAXDEV 64
+static std::mutex noalloc_lock;
+static unsigned long long *noalloc_addr[NOALLOC_MAXDEV];
+static int noalloc_nsm[NOALLOC_MAXDEV];
+
+static int noalloc_fail(const char *fmt, ...)
+{
+   va_list ap;
+   va_start(ap, fmt);
+   fprintf(stderr, "GmlxReduceNoAlloc: ");
+   vfprintf(stderr, fmt, ap);
+   fprintf(stderr, "\n");
+   va_end(ap);
+   return 0;
+}
+
+extern "C" int GmlxReduceNoAlloc(const float *DevVec, size_t NmbLin, int RedOpp,
+                                 double *res, void *stream)
+{
+   cudaStream_t st = (cudaStream_t)stream;
+   unsigned long long *scr;
+   int dev = -1, nsm, nb;
+   cudaError_t e;
+
+   if(!res)
+      return noalloc_fail("res is NULL");
+   if(RedOpp < GmlMin || RedOpp > GmlLinf)
+      return noalloc_fail("unknown reduction operation %d", RedOpp);
+   if(NmbLin > (size_t)GMLX_NOALLOC_MAX_LINES)
+      return noalloc_fail("%lld lines exceed the maximum of %lld",
+                          (long long)NmbLin, (long long)GMLX_NOALLOC_MAX_LINES);
+   if(NmbLin == 0)
+   {
+      *res = (RedOpp == GmlMin) ? (double)FLT_MAX : (RedOpp == GmlMax) ? -(double)FLT_MAX : 0.0;
+      return 1;
+   }
+   if(!DevVec)
+      return noalloc_fail("DevVec is NULL with %lld lines", (long long)NmbLin);
+
+   if((e = cudaGetDevice(&dev)) != cudaSuccess)
+      return noalloc_fail("cudaGetDevice failed (error %d)", (int)e);
+   if(dev < 0 || dev >= NOALLOC_MAXDEV)
+      return noalloc_fail("device %d is beyond the %d devices supported", dev, NOALLOC_MAXDEV);
+
+   /* first call on this device: resolve the scratch address (with the device
+      current) and the SM count; later calls read the cached values */
+   {
+      std::lock_guard<std::mutex> g(noalloc_lock);
+      if(!noalloc_addr[dev])
+      {
+         void *p = NULL;
+         if((e = cudaGetSymbolAddress(&p, gml_noalloc_scratch)) != cudaSuccess || !p)
+            return noalloc_fail("cudaGetSymbolAddress failed on device %d (error %d)", dev, (int)e);
+         if((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+            return noalloc_fail("cudaDeviceGetAttribute failed on device %d (error %d)", dev, (int)e);
+         noalloc_nsm[dev] = nsm;
+         noalloc_addr[dev] = (unsigned long long *)p;
+      }
+      scr = noalloc_addr[dev];
+      nsm = noalloc_nsm[dev];
+   }
+
+   {
+      long long want = ((long long)NmbLin + 4 * RED_THREADS - 1) / (4 * RED_THREADS);
+      long long cap = 2LL * nsm < RED_MAXBLK ? 2LL * nsm : RED_MAXBLK;
+      nb = (int)(want < cap ? want : cap);
+      if(nb < 1) nb = 1;
+   }
+
+   {
+      const int n = (int)NmbLin;
+      switch(RedOpp)
+      {
+         case 0: gml_reduce_f32_kernel<0><<<nb, RED_THREADS, 0, st>>>(DevVec, n, scr); break;
+         case 1: gml_reduce_f32_kernel<1><<<nb, RED_THREADS, 0, st>>>(DevVec, n, scr); break;
+         case 2: gml_reduce_f32_kernel<2><<<nb, RED_THREADS, 0, st>>>(DevVec, n, scr); break;
+         case 3: gml_reduce_f32_kernel<3><<<nb, RED_THREADS, 0, st>>>(DevVec, n, scr); break;
+         case 4: gml_reduce_f32_kernel<4><<<nb, RED_THREADS, 0, st>>>(DevVec, n, scr); break;
+         case 5: gml_reduce_f32_kernel<5><<<nb, RED_THREADS, 0, st>>>(DevVec, n, scr); break;
+         default: gml_reduce_f32_kernel<6><<<nb, RED_THREADS, 0, st>>>(DevVec, n, scr); break;
+      }
+   }
+   if((e = cudaGetLastError()) != cudaSuccess)
+      return noalloc_fail("launch failed (error %d)", (int)e);
+   if((e = cudaMemcpyAsync(res, scr + 1, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+      return noalloc_fail("reading the result failed (error %d)", (int)e);
+   if((e = cudaStreamSynchronize(st)) != cudaSuccess)
+      return noalloc_fail("stream synchronisation failed (error %d)", (int)e);
    return 1;
 }

@@ -105,6 +105,37 @@ int      GmlxReduceArg        (size_t, int DatIdx, float *MinVal, int *MinIdx,
                                float *MaxVal, int *MaxIdx);
 
 /* ---------------------------------------------------------------------------
+ * Reduction that allocates nothing.  No counterpart in the reference.
+ *
+ * GmlReduceVector needs an instance (GmlInit allocates its buffers) and a
+ * datatype.  Some callers cannot allocate device memory at the point where
+ * they need a reduction: a host whose own memory pool has reserved the free
+ * device memory (cudaMalloc then fails), or a time-critical loop that must
+ * not take the device-wide synchronisation cudaFree implies.  They pass a
+ * device pointer of their own instead.
+ *
+ * RedOpp is GmlMin..GmlLinf, computed as GmlReduceVector does (FP64
+ * combine; L2 is the sum of squares, no square root); *res (host) receives
+ * the result, and NmbLin = 0 gives the operation's identity.  The call
+ * launches on `stream` (a cudaStream_t, NULL for the legacy default stream)
+ * of the CURRENT device, where DevVec must live, and returns when the result
+ * is on the host: 1 on success, 0 on failure with a one-line message on
+ * stderr.  NmbLin above GMLX_NOALLOC_MAX_LINES is rejected that way.
+ *
+ * Scratch: a static device array of GMLX_NOALLOC_SCRATCH_BYTES, one per
+ * device.  It is zero when the library's device code loads and every
+ * completed call leaves it in that state; nothing needs clearing by the
+ * caller.  Its address is looked up on the first call on each device, so
+ * make that first call outside any stream capture.  Calls on one stream run
+ * one after the other and are safe; calls that overlap on one device (two
+ * streams, two host threads) share the scratch and race.
+ * ------------------------------------------------------------------------- */
+#define GMLX_NOALLOC_MAX_LINES      2147483647      /* 32-bit line index */
+#define GMLX_NOALLOC_SCRATCH_BYTES  8208            /* (2 + 1024) x 8 bytes */
+int      GmlxReduceNoAlloc    (const float *DevVec, size_t NmbLin, int RedOpp,
+                               double *res, void *stream);
+
+/* ---------------------------------------------------------------------------
  * Native tetrahedral mesh kernels: Laplacian smoothing over the ball of
  * points and mean-ratio quality statistics.  They work on the instance's
  * GmlVertices and GmlTetrahedra datatypes in place, without generated
