@@ -59,6 +59,15 @@ def parse():
     p.add_argument("--n", type=int, default=N_HEX, help="hexes per cube side")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=20)
+    p.add_argument("--workload", default="smooth", choices=["smooth", "solve", "batch", "serve"],
+                   help="smooth: the smoothing + quality step (default); solve: block SpMV "
+                        "and CG; batch: 512 meshes through the tile queue vs the per-mesh "
+                        "launch loop; serve: the request loop on a Poisson stream")
+    p.add_argument("--meshes", type=int, default=512, help="batch: number of meshes")
+    p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
+    p.add_argument("--rate", type=float, default=200.0, help="serve: requests per second")
+    p.add_argument("--serial-requests", type=int, default=200,
+                   help="serve: requests of the trace replayed on the serial plain path")
     return p.parse_args()
 
 
@@ -370,12 +379,279 @@ def run_gpu(args, dist):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------- solver workload
+
+SOLVE_N = 96
+SOLVE_TOL = 1e-10
+
+
+def run_solve(args, dist):
+    """Block SpMV and CG on the 3x3-block SPD system of the vertex graph of a
+    96^3-hex cube (912,673 rows, 13,465,441 blocks): SpMV launch times in FP32
+    and FP64 (CUDA events, 50 launches each), then FP64 CG and FP32 CG inside
+    FP64 refinement to 1e-10 relative residual (device time of each solve,
+    median of --steps solves after --warmup)."""
+    import gmlib_gb300 as G
+    n = SOLVE_N if args.n == N_HEX else args.n
+    lin, col, val, rhs = G.cube_spd(n, 0, seed=SEED)
+    nrow, nnzb = len(lin) - 1, len(col)
+    g = G.lib.GmlInit(dist.local)
+    if not g:
+        raise SystemExit("GmlInit failed")
+    G.lib.GmlxSetTiming(g, 0)
+    IP = ctypes.POINTER(ctypes.c_int)
+    lin_c, col_c = lin.ctypes.data_as(IP), col.ctypes.data_as(IP)
+    v64 = np.ascontiguousarray(val)
+    v32 = v64.astype(np.float32)
+    m64 = G.lib.GmlNewMatrix(g, nrow, nnzb, 3, G.as_ptr(v64), col_c, lin_c, G.GmlDbl)
+    m32 = G.lib.GmlNewMatrix(g, nrow, nnzb, 3, G.as_ptr(v32), col_c, lin_c, G.GmlFlt)
+    x32 = rhs.astype(np.float32)
+    vx32 = G.lib.GmlNewVector(g, nrow, 3, G.as_ptr(x32), G.GmlFlt)
+    vy32 = G.lib.GmlNewVector(g, nrow, 3, None, G.GmlFlt)
+    vb = G.lib.GmlNewVector(g, nrow, 3, G.as_ptr(rhs), G.GmlDbl)
+    vx = G.lib.GmlNewVector(g, nrow, 3, None, G.GmlDbl)
+    vy = G.lib.GmlNewVector(g, nrow, 3, None, G.GmlDbl)
+    if min(m64, m32, vx32, vy32, vb, vx, vy) <= 0:
+        raise SystemExit("allocation failed")
+
+    e0, e1 = G.lib.GmlxEventCreate(), G.lib.GmlxEventCreate()
+    peak, peak_src = peak_hbm()
+    spmv = {}
+    for name, m, y, x, byt in (("f32", m32, vy32, vx32, 40.0 * nnzb + 4.0 * (nrow + 1) + 24.0 * nrow),
+                               ("f64", m64, vy, vb, 76.0 * nnzb + 4.0 * (nrow + 1) + 48.0 * nrow)):
+        for _ in range(3):
+            G.lib.GmlMultMatVec(g, m, y, x)
+        G.lib.GmlxSynchronize(g)
+        G.lib.GmlxEventRecord(g, e0)
+        for _ in range(50):
+            G.lib.GmlMultMatVec(g, m, y, x)
+        G.lib.GmlxEventRecord(g, e1)
+        t = G.lib.GmlxEventElapsed(e0, e1) / 50
+        spmv[name] = {"mean_launch_us": round(t * 1e6, 2), "algorithmic_bytes": byt,
+                      "achieved_gbs": round(byt / t / 1e9, 1), "frac": round(byt / t / 1e9 / peak, 4),
+                      "gflops": round(18.0 * nnzb / t / 1e9, 1)}
+
+    solves = {}
+    clocks = Clocks(dist.local)
+    clocks.start()
+    for mode, name in ((G.GmlxCgFp64, "cg_fp64"), (G.GmlxCgMixed, "cg_fp32_in_fp64_ir")):
+        info = G.GmlxSolveInfo()
+        times = []
+        for i in range(args.warmup + args.steps):
+            rc = G.lib.GmlxSolveCG(g, m64, vb, vx, mode, SOLVE_TOL, 20000, ctypes.byref(info))
+            if rc != 1:
+                raise SystemExit("%s did not converge (rc %d, |r|/|b| %g)" % (name, rc, info.RelRes))
+            if i >= args.warmup:
+                times.append(info.Seconds)
+        solves[name] = {"seconds": round(statistics.median(times), 6), "iterations": info.NmbIte,
+                        "refinement_steps": info.NmbOut, "rel_residual": info.RelRes,
+                        "solves_per_s": round(1.0 / statistics.median(times), 2)}
+    clk = clocks.stop()
+    G.lib.GmlStop(g)
+    speedup = solves["cg_fp64"]["seconds"] / solves["cg_fp32_in_fp64_ir"]["seconds"]
+    ctypes.CDLL(None).fflush(None)          # the library's own messages go first
+    if dist.rank == 0:
+        line = {"metric": "CG to 1e-10: FP64 CG time / FP32-CG-in-FP64-IR time",
+                "value": round(speedup, 3), "unit": "x", "n_gpus": dist.world,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                "dtype": "f64 / f32+f64", "data": "synthetic",
+                "config": {"workload": "3x3-block SPD system on the vertex graph of a %d^3-hex "
+                                       "tet cube" % n, "rows": nrow, "blocks": nnzb,
+                           "tol": SOLVE_TOL, "inputs": "larger than L2 (FP64 matrix %.0f MB)"
+                           % (76.0 * nnzb / 1e6)},
+                "spmv": spmv, "solves": solves, "peak_gbs": peak, "peak_source": peak_src,
+                "clocks": clk}
+        print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------ batched meshes
+
+def gen_meshes(specs):
+    """specs: (n, split, jitter, seed) -> [(crd, tet, ref)], generated in
+    parallel (the library calls release the GIL)."""
+    import gmlib_gb300 as G
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(sp):
+        n, split, jit, seed = sp
+        return G.cube_mesh(n, split=split, jitter=jit, seed=seed)
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        return list(ex.map(one, specs))
+
+
+def run_batch(args, dist):
+    """512 jittered tet cubes, hexes per side log-uniform in [10, 80], reflected
+    split, Hilbert order: 5 sweeps + quality statistics (min/argmin) per mesh,
+    through one persistent tile-queue launch (CUDA graph, tuned tiles) and
+    through the per-mesh launch loop.  meshes/s over --steps runs of each."""
+    import gmlib_gb300 as G
+    rng = np.random.default_rng(SEED)
+    ns = np.exp(rng.uniform(np.log(10), np.log(80), args.meshes)).astype(int)
+    t0 = time.time()
+    ms = gen_meshes([(int(n), 1, 0.3, SEED + i) for i, n in enumerate(ns)])
+    tgen = time.time() - t0
+    nv = np.array([len(m[0]) for m in ms], np.int32)
+    nt = np.array([len(m[1]) for m in ms], np.int32)
+    h = 1.0 / ns.astype(np.float64)
+    g = G.lib.GmlInit(dist.local)
+    G.lib.GmlxSetTiming(g, 0)
+    if G.lib.GmlxBatchCreate(g, len(ms), G.as_ptr(nv), G.as_ptr(nt), G.as_ptr(h)) != 1:
+        raise SystemExit("GmlxBatchCreate failed")
+    for i, (crd, tet, ref) in enumerate(ms):
+        G.lib.GmlxBatchSetMesh(g, i, G.as_ptr(crd), G.as_ptr(ref), G.as_ptr(tet))
+    if G.lib.GmlxBatchSetup(g, 1) != 1:
+        raise SystemExit("GmlxBatchSetup failed")
+    sweeps, om = 5, ctypes.c_float(OMEGA)
+    G.lib.GmlxBatchTune(g, sweeps, om)
+    ts_, tt_, gr_, ntile = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    res = (G.GmlxQuality * len(ms))()
+    e0, e1 = G.lib.GmlxEventCreate(), G.lib.GmlxEventCreate()
+    out = {}
+    clocks = Clocks(dist.local)
+    clocks.start()
+    for name, mode in (("queue", G.GmlxBatchQueue), ("loop", G.GmlxBatchLoop)):
+        for _ in range(args.warmup):
+            G.lib.GmlxBatchRun(g, sweeps, om, mode, None)
+        G.lib.GmlxSynchronize(g)
+        G.lib.GmlxEventRecord(g, e0)
+        for _ in range(args.steps):
+            if G.lib.GmlxBatchRun(g, sweeps, om, mode, None) != 1:
+                raise SystemExit("GmlxBatchRun failed")
+        G.lib.GmlxEventRecord(g, e1)
+        t = G.lib.GmlxEventElapsed(e0, e1) / args.steps
+        out[name] = {"ms_per_run": round(t * 1e3, 3), "meshes_per_s": round(len(ms) / t, 1)}
+    clk = clocks.stop()
+    G.lib.GmlxBatchRun(g, sweeps, om, G.GmlxBatchQueue, res)
+    G.lib.GmlxBatchInfo(g, ctypes.byref(ts_), ctypes.byref(tt_), ctypes.byref(gr_),
+                        ctypes.byref(ntile))
+    stored, used, mx = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
+    G.lib.GmlxMeshBallInfo(g, ctypes.byref(stored), ctypes.byref(used), ctypes.byref(mx))
+    vpad = float(sum((int(v) + 255) // 256 * 256 for v in nv))
+    byts = sweeps * (36.0 * vpad + 4.0 * used.value) + 16.0 * nt.sum() + 16.0 * vpad \
+        + 4.0 * sum((int(t) + 31) // 32 for t in nt)
+    G.lib.GmlStop(g)
+    peak, _ = peak_hbm()
+    tq = out["queue"]["ms_per_run"] / 1e3
+    if dist.rank == 0:
+        line = {"metric": "batched meshes/s (5 sweeps + quality + min per mesh)",
+                "value": out["queue"]["meshes_per_s"], "unit": "meshes/s", "n_gpus": dist.world,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "%d jittered tet cubes, hexes per side log-uniform in "
+                                       "[10, 80], reflected split" % len(ms),
+                           "tets": int(nt.sum()), "vertices": int(nv.sum()), "sweeps": sweeps,
+                           "generation_s": round(tgen, 1)},
+                "queue": out["queue"], "loop": out["loop"],
+                "speedup_vs_loop": round(out["loop"]["ms_per_run"] / out["queue"]["ms_per_run"], 2),
+                "tiles": {"slices_per_sweep_tile": ts_.value, "tets_per_quality_tile": tt_.value,
+                          "grid": gr_.value, "tiles": ntile.value},
+                "roofline": {"bound": "hbm", "algorithmic_bytes_per_run": byts,
+                             "achieved": round(byts / tq / 1e9, 1), "peak": peak,
+                             "frac": round(byts / tq / 1e9 / peak, 4), "unit": "GB/s"},
+                "min_quality": float(min(r.MinQal for r in res)), "clocks": clk}
+        print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ serving
+
+SERVE_BUCKETS = 12
+
+
+def run_serve(args, dist):
+    """Poisson arrivals (--rate per s for --duration s), 50/30/20 quality /
+    10-sweep smoothing / CG requests on meshes of 1e4..1e7 tets (log-uniform)
+    and on the SPD systems of their vertex graphs; a request targets a mesh
+    seen before with probability 0.5, else a new one.  Distinct sizes come
+    from a pool of size buckets (each new target is a separate resident
+    copy).  Continuous batching with a 150 GB budget, then the serial plain
+    path on the first --serial-requests requests of the same trace."""
+    import gmlib_gb300 as G
+    rng = np.random.default_rng(SEED)
+    ns = np.unique(np.round(np.exp(np.linspace(np.log((1e4 / 6) ** (1 / 3)),
+                                               np.log((1e7 / 6) ** (1 / 3)),
+                                               SERVE_BUCKETS))).astype(int))
+    t0 = time.time()
+    meshes = gen_meshes([(int(n), 1, 0.3, SEED + i) for i, n in enumerate(ns)])
+    systems = [G.cube_spd(int(n), 0, seed=SEED + i) for i, n in enumerate(ns)]
+    tgen = time.time() - t0
+    logt = np.log(6.0 * ns.astype(np.float64) ** 3)
+
+    def bucket(x):
+        return int(np.argmin(np.abs(logt - x)))
+    srv = G.lib.GmlxServeNew(dist.local, 150e9, 8)
+    nreq = int(args.rate * args.duration)
+    req = (G.GmlxRequest * nreq)()
+    seen = {0: [], 1: []}
+    t = 0.0
+    kinds = []
+    for i in range(nreq):
+        t += rng.exponential(1.0 / args.rate)
+        u = rng.random()
+        kind = G.GmlxReqQuality if u < 0.5 else (G.GmlxReqSmooth if u < 0.8 else G.GmlxReqSolve)
+        cls = 1 if kind == G.GmlxReqSolve else 0
+        if seen[cls] and rng.random() < 0.5:
+            target = int(rng.choice(seen[cls]))
+        else:
+            b = bucket(rng.uniform(np.log(1e4), np.log(1e7)))
+            if cls == 0:
+                crd, tet, ref = meshes[b]
+                target = G.lib.GmlxServeAddMesh(srv, len(crd), G.as_ptr(crd), G.as_ptr(ref),
+                                                len(tet), G.as_ptr(tet), 1.0 / ns[b])
+            else:
+                lin, col, val, rhs = systems[b]
+                target = G.lib.GmlxServeAddSystem(srv, len(lin) - 1, len(col), G.as_ptr(lin),
+                                                  G.as_ptr(col), G.as_ptr(val), G.as_ptr(rhs))
+            seen[cls].append(target)
+        req[i].kind, req[i].target, req[i].arrival = kind, target, t
+        kinds.append(kind)
+    stb = G.GmlxServeStats()
+    clocks = Clocks(dist.local)
+    clocks.start()
+    G.lib.GmlxServeRun(srv, req, nreq, G.GmlxServeBatching, ctypes.byref(stb))
+    clk = clocks.stop()
+    nser = min(nreq, args.serial_requests)
+    ser = (G.GmlxRequest * max(nser, 1))()
+    for i in range(nser):
+        ser[i].kind, ser[i].target, ser[i].arrival = req[i].kind, req[i].target, req[i].arrival
+    sts = G.GmlxServeStats()
+    G.lib.GmlxServeRun(srv, ser, nser, G.GmlxServeSerial, ctypes.byref(sts))
+    same = sum(1 for i in range(nser)
+               if req[i].status == 1 and ser[i].status == 1
+               and (req[i].NmbIte, req[i].RelRes, req[i].qal.MinQal, req[i].qal.MinIdx)
+               == (ser[i].NmbIte, ser[i].RelRes, ser[i].qal.MinQal, ser[i].qal.MinIdx))
+    G.lib.GmlxServeFree(srv)
+
+    def d(st):
+        return {"completed": st.completed, "failed": st.failed, "seconds": round(st.seconds, 2),
+                "throughput_rps": round(st.throughput, 2), "p50_ms": round(st.p50 * 1e3, 2),
+                "p99_ms": round(st.p99 * 1e3, 2), "max_ms": round(st.max * 1e3, 2),
+                "loads": st.loads, "evictions": st.evictions,
+                "peak_resident_gb": round(st.peak_bytes / 1e9, 2)}
+    if dist.rank == 0:
+        line = {"metric": "served requests/s at p99 (continuous batching)",
+                "value": round(stb.throughput, 2), "unit": "req/s", "n_gpus": dist.world,
+                "higher_is_better": True, "dtype": "f32 / f64", "data": "synthetic",
+                "config": {"workload": "Poisson %.0f req/s for %.0f s, 50/30/20 quality / "
+                                       "10-sweep smoothing / CG (1e-10)" % (args.rate, args.duration),
+                           "sizes_tets": [int(6 * n ** 3) for n in ns], "reuse": 0.5,
+                           "budget_gb": 150, "slots": 8, "pool_generation_s": round(tgen, 1)},
+                "batching": d(stb), "serial_prefix": d(sts),
+                "same_result_alone_and_in_mix": "%d of %d" % (same, nser), "clocks": clk}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
         if args.impl == "reference":
             run_reference(args, dist)
+        elif args.workload == "solve":
+            run_solve(args, dist)
+        elif args.workload == "batch":
+            run_batch(args, dist)
+        elif args.workload == "serve":
+            run_serve(args, dist)
         else:
             run_gpu(args, dist)
     finally:

@@ -128,6 +128,53 @@ SIGNATURES.update({
 })
 
 
+class GmlxSolveInfo(ctypes.Structure):
+    _fields_ = [("NmbIte", ctypes.c_int), ("NmbOut", ctypes.c_int),
+                ("RelRes", ctypes.c_double), ("Seconds", ctypes.c_double)]
+
+
+GmlxCgFp64, GmlxCgMixed = 0, 1
+GmlxBatchQueue, GmlxBatchLoop = 0, 1
+GmlxReqQuality, GmlxReqSmooth, GmlxReqSolve = 0, 1, 2
+GmlxServeBatching, GmlxServeSerial = 0, 1
+
+
+class GmlxRequest(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("target", ctypes.c_int), ("arrival", ctypes.c_double),
+                ("start", ctypes.c_double), ("finish", ctypes.c_double),
+                ("status", ctypes.c_int), ("NmbIte", ctypes.c_int), ("RelRes", ctypes.c_double),
+                ("qal", GmlxQuality)]
+
+
+class GmlxServeStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_int), ("failed", ctypes.c_int), ("loads", ctypes.c_int),
+                ("evictions", ctypes.c_int), ("seconds", ctypes.c_double),
+                ("throughput", ctypes.c_double), ("mean", ctypes.c_double),
+                ("p50", ctypes.c_double), ("p99", ctypes.c_double), ("max", ctypes.c_double),
+                ("peak_bytes", ctypes.c_double)]
+SIGNATURES.update({
+    "GmlxSolveCG": (_i, [_s, _i, _i, _i, _i, _d, _i, ctypes.POINTER(GmlxSolveInfo)]),
+    "GmlxCubeSpdSizes": (_i, [_i, _i, _ip, _ip]),
+    "GmlxVectorData": (_i, [_s, _i]),
+    "GmlxBatchCreate": (_i, [_s, _i, _p, _p, _p]),
+    "GmlxBatchSetMesh": (_i, [_s, _i, _p, _p, _p]),
+    "GmlxBatchSetup": (_i, [_s, _i]),
+    "GmlxBatchRun": (_i, [_s, _i, _f, _i, ctypes.POINTER(GmlxQuality)]),
+    "GmlxBatchGetMesh": (_i, [_s, _i, _p]),
+    "GmlxBatchFlags": (_i, [_s, _i, _p, _s]),
+    "GmlxBatchTune": (_i, [_s, _i, _f]),
+    "GmlxBatchInfo": (_i, [_s, _ip, _ip, _ip, _ip]),
+    "GmlxServeNew": (_s, [_i, _d, _i]),
+    "GmlxServeAddMesh": (_i, [_s, _i, _p, _p, _i, _p, _d]),
+    "GmlxServeAddSystem": (_i, [_s, _i, _i, _p, _p, _p, _p]),
+    "GmlxServeRun": (_i, [_s, _p, _i, _i, _p]),
+    "GmlxServeResident": (_i, [_s, _dp]),
+    "GmlxServeTargetBytes": (_d, [_s, _i]),
+    "GmlxServeFree": (None, [_s]),
+    "GmlxCubeSpdMatrix": (_i, [_i, _i, ctypes.c_uint64, _p, _p, _p, _p]),
+})
+
+
 def _load():
     if not os.path.exists(LIB_PATH):
         raise ImportError("libgmlib3.so is not built: run `python -m gmlib_gb300.build` "
@@ -202,6 +249,21 @@ def get_data(g, idx, dtype, shape):
     if not ok:
         raise RuntimeError("GmlxGetData failed for datatype %d" % idx)
     return out
+
+
+def cube_spd(n, split=0, seed=7):
+    """Block CSR system of GmlxCubeSpdMatrix: (lin, col, val[nnzb,3,3], rhs[nv,3])."""
+    nl, nb = ctypes.c_int(), ctypes.c_int()
+    if not lib.GmlxCubeSpdSizes(n, split, ctypes.byref(nl), ctypes.byref(nb)):
+        raise ValueError("bad cube size")
+    lin = np.zeros(nl.value + 1, np.int32)
+    col = np.zeros(nb.value, np.int32)
+    val = np.zeros((nb.value, 3, 3), np.float64)
+    rhs = np.zeros((nl.value, 3), np.float64)
+    if not lib.GmlxCubeSpdMatrix(n, split, int(seed), as_ptr(lin), as_ptr(col), as_ptr(val),
+                                 as_ptr(rhs)):
+        raise RuntimeError("GmlxCubeSpdMatrix failed")
+    return lin, col, val, rhs
 
 
 def upload_mesh(g, crd, tet, ref=None):

@@ -271,6 +271,12 @@ extern "C" int gmd_d2h(GmdCtx *ctx, void *dst, const void *src, size_t bytes)
    return ok(ctx, cudaStreamSynchronize(ctx->stream), "download synchronize");
 }
 
+extern "C" int gmd_d2h_async(GmdCtx *ctx, void *dst, const void *src, size_t bytes)
+{
+   if(!ctx) { memcpy(dst, src, bytes); return 1; }
+   return ok(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download");
+}
+
 extern "C" int gmd_d2d_async(GmdCtx *ctx, void *dst, const void *src, size_t bytes)
 {
    if(!ctx) { memmove(dst, src, bytes); return 1; }

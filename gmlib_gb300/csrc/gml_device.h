@@ -42,6 +42,7 @@ void    *gmd_host_alloc(size_t bytes);                    /* pinned, zeroed */
 void     gmd_host_free(void *ptr);
 int      gmd_h2d_async(GmdCtx *ctx, void *dst, const void *src, size_t bytes);
 int      gmd_d2h(GmdCtx *ctx, void *dst, const void *src, size_t bytes);
+int      gmd_d2h_async(GmdCtx *ctx, void *dst, const void *src, size_t bytes);
 int      gmd_d2d_async(GmdCtx *ctx, void *dst, const void *src, size_t bytes);
 int      gmd_memset_async(GmdCtx *ctx, void *dst, int val, size_t bytes);
 

@@ -44,10 +44,12 @@ int gmlx_timing_off(GmlSct *gml)
 }
 
 void gmlx_native_release(GmlSct *gml);
+void gmlx_batch_release(GmlSct *gml);
 
 void gmlx_release_extensions(GmlSct *gml)
 {
    int i;
+   gmlx_batch_release(gml);
    gmlx_native_release(gml);
    for(i=0;i<gml->NmbNames;i++)
       free(gml->Names[i]);

@@ -77,6 +77,7 @@ typedef struct
    int         *RowPtr, *ColIdx;
    void        *Val;
    float       FltOpp, MemAcc;
+   void        *Sol;                  /* solver work space (gml_solver.c) */
 }GmlMatSct;
 
 typedef struct
@@ -111,9 +112,11 @@ typedef struct
    int         LazyOff;               /* 1: always emit eager prologues */
    int         TimOff;                /* 1: no per-launch timing events */
    int         Offline;               /* 1: no GPU, code generation only */
+   int         Quiet;                 /* 1: no informational messages */
    char        **Names;               /* interned strings owned by the instance */
    int         NmbNames, CapNames;
    void        *ext;                  /* state of the native extensions */
+   void        *bat;                  /* batched meshes (gml_batch.c) */
 }GmlSct;
 
 #define GETGMLPTR(p,i)  GmlSct *p = (GmlSct *)(i)

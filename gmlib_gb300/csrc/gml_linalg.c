@@ -150,6 +150,7 @@ int gml_sell_upload(GmlSct *gml, const GmlSell *s, GmlSellDev *d)
    d->BlkSiz = s->BlkSiz;
    d->FltSiz = s->FltSiz;
    d->NmbSlc = s->NmbSlc;
+   d->NmbCol = s->NmbCol;
    d->bytes  = (size_t)(s->NmbSlc + 1) * 8 + (size_t)s->NmbLin * 4
              + s->NmbCol * 32 * 4 + s->NmbCol * 32 * bb * s->FltSiz;
    d->SlcOff = gmd_alloc(gml->dev, (size_t)(s->NmbSlc + 1) * 8);
@@ -223,9 +224,12 @@ int GmlNewMatrix(size_t GmlIdx, int NmbLin, int NmbBlk, int BlkSiz, void *val,
       return 0;
    }
 
-   printf(" Matrix slices = %d (SELL-32)\n", sell.NmbSlc);
-   printf("  sparse nnz = %d, vectorized nnz = %zu, occupency = %.1f%%\n",
-          NmbBlk, sell.NmbCol * 32, (100. * NmbBlk) / (double)(sell.NmbCol * 32));
+   if(!gml->Quiet)
+   {
+      printf(" Matrix slices = %d (SELL-32)\n", sell.NmbSlc);
+      printf("  sparse nnz = %d, vectorized nnz = %zu, occupency = %.1f%%\n",
+             NmbBlk, sell.NmbCol * 32, (100. * NmbBlk) / (double)(sell.NmbCol * 32));
+   }
 
    gml_sell_free(&sell);
    mat->Val = dev;
@@ -234,7 +238,8 @@ int GmlNewMatrix(size_t GmlIdx, int NmbLin, int NmbBlk, int BlkSiz, void *val,
 
    mat->MemAcc = ((float)NmbLin * BlkSiz + (float)NmbBlk * BlkSiz * (BlkSiz + 1)) * FltSiz;
    mat->FltOpp = (float)NmbBlk * BlkSiz * BlkSiz * 2;
-   printf("  swipe = %.2f GB, %.2f GFlops\n", mat->MemAcc / 1.E9, mat->FltOpp / 1.E9);
+   if(!gml->Quiet)
+      printf("  swipe = %.2f GB, %.2f GFlops\n", mat->MemAcc / 1.E9, mat->FltOpp / 1.E9);
 
    return MatIdx;
 }
@@ -300,6 +305,16 @@ int GmlNewVector(size_t GmlIdx, int NmbLin, int BlkSiz, void *val, int FltTyp)
    vec->idx = DatIdx;
    gml_upload(gml, DatIdx);
    return VecIdx;
+}
+
+/* datatype holding the lines of a vector (the reference keeps it in
+   vec->idx, sources/gmlib3.c:1504, without exposing it) */
+int GmlxVectorData(size_t GmlIdx, int VecIdx)
+{
+   GETGMLPTR(gml, GmlIdx);
+   if(VecIdx < 1 || VecIdx > GmlMaxVec || !gml->vec[VecIdx].use)
+      return 0;
+   return gml->vec[VecIdx].idx;
 }
 
 /* ========================================================================= */

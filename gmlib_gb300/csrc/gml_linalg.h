@@ -31,6 +31,7 @@ typedef struct
 {
    int      NmbLin, BlkSiz, FltSiz, NmbSlc;
    size_t   bytes;
+   size_t   NmbCol;          /* sum of slice widths */
    int64_t  *SlcOff;
    int      *Deg, *Col;
    void     *Val;
@@ -60,6 +61,7 @@ void gml_sell_free(GmlSell *s);
 int  gml_sell_upload(GmlSct *gml, const GmlSell *s, GmlSellDev *d);
 void gml_sell_dev_free(GmlSct *gml, GmlSellDev *d);
 void gml_release_matrices(GmlSct *gml);
+void gml_release_solvers(GmlSct *gml);
 #endif
 
 #endif

@@ -31,6 +31,34 @@ int gmd_mesh_stats_init(struct GmdCtx *ctx, GmlxQualStats *st, int n);
 int gmd_mesh_quality(struct GmdCtx *ctx, int nt, const void *tet, const void *crd, float thr,
                      float *qout, unsigned *flags, GmlxQualStats *st, int *err);
 
+/* batched meshes (gml_batch.c): a (mesh, range) tile queue drained by one
+   persistent launch */
+typedef struct { int phase, mesh, beg, end; } GmdBatchTile;     /* phase < nsweep: slices */
+typedef struct { int t0, nt, f0, s0, s1; float thr; } GmdBatchMesh;
+typedef struct
+{
+   int                  ntile, nsweep, nmesh, nphase;
+   const GmdBatchTile   *tiles;
+   const GmdBatchMesh   *mesh;
+   const int            *need;       /* tiles per (mesh, phase) */
+   int                  *done;       /* finished tiles per (mesh, phase) */
+   int                  *head, *abort, *err;
+   const unsigned       *rowv;
+   const long long      *soff;
+   const int            *col;
+   void                 *buf0, *buf1;
+   const void           *tet;
+   unsigned             *flags;
+   GmlxQualStats        *stats;
+   float                omega;
+}GmdBatchArgs;
+
+int gmd_batch_queue(struct GmdCtx *ctx, const GmdBatchArgs *a, int grid);
+int gmd_batch_grid(struct GmdCtx *ctx);
+int gmd_mesh_laplace_slices(struct GmdCtx *ctx, int s0, int s1, const unsigned *rowv,
+                            const long long *soff, const int *col, const void *in, void *out,
+                            float omega);
+
 /* CUDA graphs on the instance stream */
 int  gmd_graph_begin(struct GmdCtx *ctx);
 int  gmd_graph_end(struct GmdCtx *ctx, void **exec);

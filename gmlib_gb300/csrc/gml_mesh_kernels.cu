@@ -612,20 +612,37 @@ __device__ __noinline__ int det64_positive(const float4 a, const float4 b, const
    return dd > 0.;
 }
 
+/* coordinate loads: through L1 (read-only path) within one kernel, or at L2
+   (.cg) when other blocks of the same launch wrote them */
+template<bool CG> __device__ __forceinline__ float4 ld_crd(const float4 *p)
+{
+   return CG ? __ldcg(p) : __ldg(p);
+}
+
+template<bool CG = false>
 __device__ __forceinline__ float tet_mean_ratio(const int4 e, const float4 *__restrict__ crd,
                                                 float thr, int *inv, int *f64)
 {
-   const float4 a = __ldg(&crd[e.x]), b = __ldg(&crd[e.y]);
-   const float4 c = __ldg(&crd[e.z]), d = __ldg(&crd[e.w]);
+   const float4 a = ld_crd<CG>(&crd[e.x]), b = ld_crd<CG>(&crd[e.y]);
+   const float4 c = ld_crd<CG>(&crd[e.z]), d = ld_crd<CG>(&crd[e.w]);
    const float abx = b.x - a.x, aby = b.y - a.y, abz = b.z - a.z;
    const float acx = c.x - a.x, acy = c.y - a.y, acz = c.z - a.z;
    const float adx = d.x - a.x, ady = d.y - a.y, adz = d.z - a.z;
+#if QK_L2ID
+   /* sum over the 6 edges of |xi - xj|^2 = 4 sum |xi|^2 - |sum xi|^2 with a
+      as the origin (4 points) */
+   const float sx = abx + acx + adx, sy = aby + acy + ady, sz = abz + acz + adz;
+   const float n2 = abx*abx + aby*aby + abz*abz + acx*acx + acy*acy + acz*acz
+                  + adx*adx + ady*ady + adz*adz;
+   const float l2 = 4.0f * n2 - (sx*sx + sy*sy + sz*sz);
+#else
    const float bcx = acx - abx, bcy = acy - aby, bcz = acz - abz;
    const float bdx = adx - abx, bdy = ady - aby, bdz = adz - abz;
    const float cdx = adx - acx, cdy = ady - acy, cdz = adz - acz;
    const float l2 = abx*abx + aby*aby + abz*abz + acx*acx + acy*acy + acz*acz
                   + adx*adx + ady*ady + adz*adz + bcx*bcx + bcy*bcy + bcz*bcz
                   + bdx*bdx + bdy*bdy + bdz*bdz + cdx*cdx + cdy*cdy + cdz*cdz;
+#endif
    float det = abx * (acy * adz - acz * ady) + aby * (acz * adx - acx * adz)
              + abz * (acx * ady - acy * adx);
    int pos = det > 0.f;
@@ -664,15 +681,29 @@ __device__ __forceinline__ void qacc_add(QAcc &a, float q, int t, int f64)
    a.nf64 += f64;
 }
 
-/* histogram update of a warp: lanes with the same bin add once */
+#ifndef QK_HIST
+#define QK_HIST 0
+#endif
+#ifndef QK_L2ID
+#define QK_L2ID 0
+#endif
+
+/* histogram update of a warp.  QK_HIST 0: lanes with the same bin add once
+   (match_any leaders); 1: one shared atomic per tet */
 __device__ __forceinline__ void hist_add_warp(unsigned *hist, float q, int valid, int lane)
 {
    int bin = (int)(q * 64.0f);
    bin = bin < 0 ? 0 : (bin > 63 ? 63 : bin);
+#if QK_HIST == 1
+   (void)lane;
+   if(valid)
+      atomicAdd(&hist[bin], 1u);
+#else
    if(!valid) bin = 64 + lane;
    const unsigned peers = __match_any_sync(0xffffffffu, bin);
    if(valid && lane == __ffs(peers) - 1)
       atomicAdd(&hist[bin], (unsigned)__popc(peers));
+#endif
 }
 
 /* block reduction of the accumulators into the global statistics */
@@ -998,5 +1029,213 @@ extern "C" int gmd_mesh_quality(GmdCtx *ctx, int nt, const void *tet, const void
    else
       tet_quality_tma_kernel<false><<<g, MK_THREADS, QK_SMEM, s>>>(nt, (const int4 *)tet,
          (const float4 *)crd, thr, qout, flags, st, err);
+   return cudaGetLastError() == cudaSuccess;
+}
+
+/* ========================================================================= */
+/* batched meshes: one persistent launch over a (mesh, range) tile queue      */
+/* ========================================================================= */
+
+/* Tiles are claimed in queue order with one atomic per tile.  The queue is
+   phase-major (every sweep-0 tile of every mesh, then sweep 1, ..., then the
+   quality tiles), and a tile of phase p of mesh m starts only when all tiles
+   of phase p - 1 of mesh m are done (per-(mesh, phase) counters).  A waiting
+   tile only depends on tiles claimed before it, by blocks that are running,
+   so the queue always drains; the wait is nevertheless bounded and a
+   timeout aborts the launch with error bit 16.
+
+   Coordinates written by other blocks of the same launch are read at L2
+   (ld.global.cg), never through L1.  Sweep tiles are whole slices of the
+   SELL ball of points (a mesh's vertex range starts on a window boundary, so
+   slices never mix meshes); quality tiles are tet ranges of one mesh starting
+   at a multiple of 32, so each warp's ballot is one flag word of that mesh. */
+
+#define BQ_SPIN (1 << 22)
+
+__device__ __forceinline__ void batch_sweep_slices(int s0, int s1, const unsigned *__restrict__ rowv,
+                                                   const long long *__restrict__ soff,
+                                                   const int *__restrict__ col,
+                                                   const float4 *in, float4 *out, float omega)
+{
+   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+   for(int sl=s0+wid; sl<s1; sl+=MK_THREADS/32)
+   {
+      const unsigned pk = __ldg(&rowv[ sl * 32 + lane ]);
+      if(pk == ROW_NONE)
+         continue;
+      const int v = (int)(pk & ROW_MASK), d = (int)(pk >> ROW_SHIFT);
+      const float4 p = __ldcg(&in[v]);
+      if(d == 0)
+      {
+         out[v] = p;
+         continue;
+      }
+      const int *cp = col + __ldg(&soff[sl]) * 32 + lane;
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      int c[8];
+#pragma unroll
+      for(int u=0;u<8;u++)
+         c[u] = u < d ? __ldg(cp + u * 32) : 0;
+      for(int k=0;k<d;k+=8)
+      {
+         int nc[8];
+#pragma unroll
+         for(int u=0;u<8;u++)
+            nc[u] = k + 8 + u < d ? __ldg(cp + (size_t)(k + 8 + u) * 32) : 0;
+#pragma unroll
+         for(int u=0;u<8;u++)
+            if(k + u < d)
+            {
+               const float4 q = __ldcg(&in[ c[u] ]);
+               sx += q.x; sy += q.y; sz += q.z;
+            }
+#pragma unroll
+         for(int u=0;u<8;u++)
+            c[u] = nc[u];
+      }
+      const float inv = 1.0f / (float)d;
+      out[v] = make_float4(p.x + omega * (sx * inv - p.x), p.y + omega * (sy * inv - p.y),
+                           p.z + omega * (sz * inv - p.z), 0.f);
+   }
+}
+
+/* quality of local tets [beg, end) of one mesh; accumulators in a and hist */
+__device__ __forceinline__ void batch_quality_range(int beg, int end, const int4 *__restrict__ tet,
+                                                    const float4 *crd, float thr,
+                                                    unsigned *__restrict__ flags, QAcc &a,
+                                                    unsigned *hist)
+{
+   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+   for(int base=beg+wid*32; base<end; base+=MK_THREADS)
+   {
+      const int j = base + lane;
+      const bool v = j < end;
+      int inv = 0, f = 0;
+      float q = 0.f;
+      if(v)
+      {
+         q = tet_mean_ratio<true>(__ldg(&tet[j]), crd, thr, &inv, &f);
+         if(q < a.mn) { a.mn = q; a.mi = j; }
+         if(q > a.mx) { a.mx = q; a.xi = j; }
+         const float tt = a.s + q, bp = tt - a.s;
+         a.c += (a.s - (tt - bp)) + (q - bp);
+         a.s = tt;
+         a.nf64 += f;
+         int bin = (int)(q * 64.0f);
+         bin = bin < 0 ? 0 : (bin > 63 ? 63 : bin);
+         atomicAdd(&hist[bin], 1u);
+      }
+      const unsigned w = __ballot_sync(0xffffffffu, inv);
+      if(lane == 0)
+      {
+         a.ninv += __popc(w);
+         flags[ base >> 5 ] = w;
+      }
+   }
+}
+
+__global__ void __launch_bounds__(MK_THREADS)
+batch_queue_kernel(GmdBatchArgs a)
+{
+   __shared__ int s_tile;
+   __shared__ unsigned hist[64];
+   QAcc acc = { 3.402823466e38f, -3.402823466e38f, 0.f, 0.f, -1, -1, 0u, 0u };
+
+   if(threadIdx.x < 64)
+      hist[threadIdx.x] = 0;
+   for(;;)
+   {
+      __syncthreads();
+      if(threadIdx.x == 0)
+      {
+         int t = -1;
+         if(!*(volatile int *)a.abort)
+            t = atomicAdd(a.head, 1);
+         if(t >= a.ntile)
+            t = -1;
+         if(t >= 0)
+         {
+            const GmdBatchTile tl = a.tiles[t];
+            if(tl.phase > 0)
+            {
+               const int k = tl.mesh * a.nphase + tl.phase - 1, need = a.need[k];
+               volatile int *dp = a.done + k;
+               int it = 0;
+               while(*dp < need)
+               {
+                  if(++it > BQ_SPIN || *(volatile int *)a.abort)
+                  {
+                     atomicOr(a.err, 16);
+                     *(volatile int *)a.abort = 1;
+                     t = -1;
+                     break;
+                  }
+                  __nanosleep(256);
+               }
+               __threadfence();
+            }
+         }
+         s_tile = t;
+      }
+      __syncthreads();
+      const int t = s_tile;
+      if(t < 0)
+         break;
+      const GmdBatchTile tl = a.tiles[t];
+      const GmdBatchMesh m = a.mesh[tl.mesh];
+      float4 *b0 = (float4 *)a.buf0, *b1 = (float4 *)a.buf1;
+      if(tl.phase < a.nsweep)
+      {
+         const float4 *in = (tl.phase & 1) ? b1 : b0;
+         float4 *out = (tl.phase & 1) ? b0 : b1;
+         batch_sweep_slices(tl.beg, tl.end, a.rowv, a.soff, a.col, in, out, a.omega);
+      }
+      else
+      {
+         const float4 *crd = (a.nsweep & 1) ? b1 : b0;
+         batch_quality_range(tl.beg, tl.end, (const int4 *)a.tet + m.t0, crd, m.thr, a.flags + m.f0,
+                             acc, hist);
+         qacc_flush(acc, hist, a.stats + tl.mesh);
+         __syncthreads();
+         if(threadIdx.x < 64)
+            hist[threadIdx.x] = 0;
+         acc = QAcc{ 3.402823466e38f, -3.402823466e38f, 0.f, 0.f, -1, -1, 0u, 0u };
+      }
+      /* every thread's writes are visible at GPU scope before the tile counts */
+      __threadfence();
+      __syncthreads();
+      if(threadIdx.x == 0)
+         atomicAdd(a.done + tl.mesh * a.nphase + tl.phase, 1);
+   }
+}
+
+extern "C" int gmd_batch_queue(GmdCtx *ctx, const GmdBatchArgs *a, int grid)
+{
+   cudaStream_t s = (cudaStream_t)gmd_stream(ctx);
+   batch_queue_kernel<<<grid, MK_THREADS, 0, s>>>(*a);
+   return cudaGetLastError() == cudaSuccess;
+}
+
+extern "C" int gmd_batch_grid(GmdCtx *ctx)
+{
+   int per = 0;
+   if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_queue_kernel, MK_THREADS, 0)
+      != cudaSuccess || per < 1)
+      per = 1;
+   return per * gmd_num_sms(ctx);
+}
+
+/* per-mesh launch loop pieces: the sweep of a slice range, the quality of one mesh */
+extern "C" int gmd_mesh_laplace_slices(GmdCtx *ctx, int s0, int s1, const unsigned *rowv,
+                                       const long long *soff, const int *col, const void *in,
+                                       void *out, float omega)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   const int ns = s1 - s0;
+   unsigned g = (unsigned)((ns + MK_THREADS / 32 - 1) / (MK_THREADS / 32));
+   if(ns <= 0)
+      return 1;
+   laplace_pf_kernel<8><<<g, MK_THREADS, 0, st>>>(ns, rowv + (size_t)s0 * 32, soff + s0, col,
+      (const float4 *)in, (float4 *)out, omega);
    return cudaGetLastError() == cudaSuccess;
 }

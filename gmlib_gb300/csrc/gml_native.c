@@ -11,32 +11,9 @@
 #include "gmlib3_gb300.h"
 #include "gml_mesh.h"
 
-#define GML_MAXSTATS 64
+#include "gml_native.h"
 
-typedef struct
-{
-   int         nv, nt, fix, ready;
-   int         nrow;                  /* rows of the SELL layout (windows x 256) */
-   int         *ptr, *vt, *tmp, *err, *fixed, *pdeg, *pcol;
-   unsigned    *rowv;
-   long long   *width, *soff;
-   long long   used, stored;
-   int         maxdeg;
-   void        *crd2;                 /* second coordinate buffer */
-   unsigned    *flags;                /* inverted-element bits */
-   GmlxQualStats *stats;              /* device, GML_MAXSTATS entries */
-   int         nstats;
-   void        *graph;                /* smoothing workload graph */
-   int         gsweeps;
-   float       gomega;
-   double      gh;
-   void        *gver, *gtet;          /* buffers the graph was captured on */
-   void        *evL[GML_MAXSTATS + 1], *evQ[GML_MAXSTATS + 1];   /* graph ordering */
-   int         NmbLoopKrn, NmbSweepKrn, NmbQalKrn;
-}NatSct;
-
-
-static NatSct *nat(GmlSct *gml)
+NatSct *gmlx_nat(GmlSct *gml)
 {
    if(!gml->ext)
       gml->ext = calloc(1, sizeof(NatSct));
@@ -95,7 +72,7 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
    if(gml->Offline || !mesh_dat(gml, &ver, &tet))
       return 0;
 
-   n = nat(gml);
+   n = gmlx_nat(gml);
    free_state(gml, n);
    nv = ver->NmbLin;
    nt = tet->NmbLin;
@@ -261,7 +238,7 @@ int GmlxSmooth(size_t GmlIdx, int nsweeps, float omega)
    return 1;
 }
 
-static void decode(const GmlxQualStats *s, GmlxQuality *r)
+void gmlx_decode_stats(const GmlxQualStats *s, GmlxQuality *r)
 {
    unsigned kmin = (unsigned)(s->MinKey >> 32), kmax = ~(unsigned)(s->MaxKey >> 32);
    unsigned umin = (kmin & 0x80000000u) ? (kmin & 0x7fffffffu) : ~kmin;
@@ -287,7 +264,7 @@ static int device_errors(GmlSct *gml, NatSct *n)
    return err;
 }
 
-static float det_threshold(double h)
+float gmlx_det_threshold(double h)
 {
    return (float)(1e-6 * h * h * h);
 }
@@ -313,7 +290,7 @@ int GmlxQualityStats(size_t GmlIdx, double h, int QalIdx, GmlxQuality *res)
       n->NmbQalKrn = gml_new_kernel_slot(gml, GmlKrnGenerated + 100, "tet_quality");
    gml_lib_timer_begin(gml, &gml->krn[ n->NmbQalKrn ]);
    gmd_mesh_stats_init(gml->dev, n->stats, 1);
-   if(!gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, ver->GpuMem, det_threshold(h),
+   if(!gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, ver->GpuMem, gmlx_det_threshold(h),
                         q ? (float *)q->GpuMem : NULL, n->flags, n->stats, n->err))
       return 0;
    gml_lib_timer_end(gml, &gml->krn[ n->NmbQalKrn ]);
@@ -321,7 +298,7 @@ int GmlxQualityStats(size_t GmlIdx, double h, int QalIdx, GmlxQuality *res)
    {
       if(!gmd_d2h(gml->dev, &st, n->stats, sizeof(st)) || (device_errors(gml, n) & 4))
          return 0;
-      decode(&st, res);
+      gmlx_decode_stats(&st, res);
    }
    return 1;
 }
@@ -376,7 +353,7 @@ int GmlxSmoothQualityLoop(size_t GmlIdx, int nsweeps, float omega, double h, Gml
          void *xs = (s & 1) ? b : a, *xn = (s & 1) ? a : b;
          gmd_use_side(gml->dev, 1);
          gmd_stream_wait(gml->dev, n->evL[s]);
-         gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, xs, det_threshold(h), NULL, n->flags,
+         gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, xs, gmlx_det_threshold(h), NULL, n->flags,
                           n->stats + s - 1, n->err);
          gmd_event_record(gml->dev, n->evQ[s]);
          gmd_use_side(gml->dev, 0);
@@ -417,7 +394,7 @@ int GmlxSmoothQualityLoop(size_t GmlIdx, int nsweeps, float omega, double h, Gml
          return 0;
       }
       for(int s=0;s<nsweeps;s++)
-         decode(&st[s], &res[s]);
+         gmlx_decode_stats(&st[s], &res[s]);
       free(st);
    }
    return 1;

@@ -1,0 +1,507 @@
+/*
+ * gml_solver_kernels.cu -- kernels of the conjugate-gradient solvers.
+ *
+ * The reference has no Krylov solver: its LinearSolver example iterates a
+ * fixed-point (Jacobi-like) update with GmlMultMatVec, GmlMultDiagMatVec and
+ * GmlAddVec3 (examples/LinearSolver/LinearSolver.c:300-338).  These kernels
+ * run CG on the same SELL-32 block matrices (gml_linalg.c) in two forms:
+ *
+ *   FP64       matrix, vectors and dots in FP64;
+ *   refinement FP32 matrix copy and FP32 vectors inside the CG iterations,
+ *              dots accumulated in FP64, and an FP64 outer loop that keeps x,
+ *              recomputes the true residual b - A x with the FP64 matrix and
+ *              restarts the FP32 CG on it.
+ *
+ * Three kernels make an iteration:
+ *
+ *   spmv_dot   q = A p and p.q, one thread per block row, the SELL-32 entry
+ *              runs read as 128-byte lines, p lines gathered through L2 with
+ *              16-byte loads; the last block to finish sets alpha = rr / p.q;
+ *   update     x += alpha p, r -= alpha q and |r|^2; the last block sets
+ *              beta, rr and the stop flag;
+ *   dir        p = r + beta p.
+ *
+ * Every kernel returns at once when the stop flag is set, so a CUDA graph of
+ * a fixed number of iterations can be replayed past convergence.  The dots
+ * are deterministic: per-block partials are folded in a fixed order.
+ *
+ * Vectors keep GmlNewVector's padded lines (4 lanes for b <= 4, 8 for
+ * b <= 8).  HBM bytes per iteration (n = lanes * rows scalars, s = scalar
+ * size): spmv_dot = matrix (4 + s b^2 per stored block, 4 per row) + 2 n s,
+ * update = 6 n s, dir = 3 n s.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "gml_device.h"
+#include "gml_solver.h"
+
+#define SV_THREADS 256
+
+__device__ __forceinline__ double sv_warp_sum(double v)
+{
+   for(int o=16;o>0;o>>=1)
+      v += __shfl_xor_sync(0xffffffffu, v, o);
+   return v;
+}
+
+/* block sum of v into thread 0 */
+__device__ __forceinline__ double sv_block_sum(double v)
+{
+   __shared__ double sh[SV_THREADS / 32];
+   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+   v = sv_warp_sum(v);
+   __syncthreads();
+   if(lane == 0)
+      sh[wid] = v;
+   __syncthreads();
+   v = 0.;
+   if(wid == 0)
+   {
+      v = lane < SV_THREADS / 32 ? sh[lane] : 0.;
+      v = sv_warp_sum(v);
+   }
+   return v;
+}
+
+/* grid sum: every block contributes v; returns 1 in thread 0 of the last
+   block to arrive, with *tot the sum of the per-block partials in block
+   order */
+__device__ __forceinline__ int sv_grid_sum(double v, double *part, GmdSvScal *sc, double *tot)
+{
+   __shared__ int last;
+   v = sv_block_sum(v);
+   if(threadIdx.x == 0)
+   {
+      part[ blockIdx.x ] = v;
+      __threadfence();
+      last = (atomicAdd(&sc->ticket, 1ULL) == (unsigned long long)(gridDim.x - 1));
+   }
+   __syncthreads();
+   if(!last)
+      return 0;
+   __threadfence();
+   v = 0.;
+   for(int i=threadIdx.x;i<(int)gridDim.x;i+=blockDim.x)
+      v += ((volatile double *)part)[i];
+   v = sv_block_sum(v);
+   if(threadIdx.x != 0)
+      return 0;
+   sc->ticket = 0ULL;
+   *tot = v;
+   return 1;
+}
+
+__device__ __forceinline__ int sv_stopped(const GmdSvScal *sc)
+{
+   return *(volatile const int *)&sc->done;
+}
+
+/* ------------------------------------------------------------------------- */
+/* vectors are padded lines of VS scalars (VS = 4 for b <= 4, 8 for b <= 8),   */
+/* the layout of GmlNewVector, so that a line is one or two 16-byte loads and */
+/* the flat vector kernels run on 16-byte chunks; padding lanes stay zero     */
+/* ------------------------------------------------------------------------- */
+
+template<class T> struct Vec16;
+template<> struct Vec16<float>  { typedef float4  type; static constexpr int n = 4; };
+template<> struct Vec16<double> { typedef double2 type; static constexpr int n = 2; };
+
+template<class T> __device__ __forceinline__ T lane(const typename Vec16<T>::type &v, int i)
+{
+   return reinterpret_cast<const T *>(&v)[i];
+}
+
+template<class T> __device__ __forceinline__ double dot16(const typename Vec16<T>::type &a,
+                                                          const typename Vec16<T>::type &b)
+{
+   double s = 0.;
+#pragma unroll
+   for(int i=0;i<Vec16<T>::n;i++)
+      s += (double)lane<T>(a, i) * (double)lane<T>(b, i);
+   return s;
+}
+
+template<class VT>
+__global__ void __launch_bounds__(SV_THREADS)
+sv_init_kernel(size_t n, int B, int VS, const double *__restrict__ bsrc,
+               double *__restrict__ b64, VT *__restrict__ x, VT *__restrict__ r,
+               VT *__restrict__ p, double *part, GmdSvScal *sc, double tol2, int maxit)
+{
+   double acc = 0., tot;
+   for(size_t i=(size_t)blockIdx.x*blockDim.x+threadIdx.x;i<n;i+=(size_t)gridDim.x*blockDim.x)
+   {
+      const double v = (int)(i % (size_t)VS) < B ? bsrc[i] : 0.;   /* padding lanes are zero */
+      if(b64) b64[i] = v;
+      x[i] = (VT)0;
+      r[i] = (VT)v;
+      p[i] = (VT)v;
+      acc += v * v;
+   }
+   if(sv_grid_sum(acc, part, sc, &tot))
+   {
+      sc->bb = tot;
+      sc->rr = tot;
+      sc->rt = tot;
+      sc->stop = tol2 * tot;
+      sc->it = 0;
+      sc->maxit = maxit;
+      sc->done = tot > 0. ? 0 : 1;
+   }
+}
+
+/* y = A x for the block row r (one thread per row); x lines of VS scalars */
+template<int B, int VS, class T>
+__device__ __forceinline__ void sv_row_product(int r, const int64_t *__restrict__ soff,
+                                               const int *__restrict__ deg,
+                                               const int *__restrict__ col,
+                                               const T *__restrict__ val,
+                                               const T *__restrict__ x, T y[VS])
+{
+   typedef typename Vec16<T>::type V;
+   constexpr int NV = VS / Vec16<T>::n;
+   const int lane_ = r & 31;
+   const int64_t base = __ldg(&soff[ r >> 5 ]);
+   const int d = __ldg(&deg[r]);
+   const int *cp = col + base * 32 + lane_;
+   const T *vp = val + base * (B * B * 32) + lane_;
+#pragma unroll
+   for(int i=0;i<VS;i++)
+      y[i] = (T)0;
+#pragma unroll 2
+   for(int k=0;k<d;k++)
+   {
+      const int c = __ldg(cp + (size_t)k * 32);
+      T xv[VS];
+      const V *xp = reinterpret_cast<const V *>(x + (size_t)c * VS);
+#pragma unroll
+      for(int u=0;u<NV;u++)
+      {
+         const V t = __ldg(xp + u);
+#pragma unroll
+         for(int i=0;i<Vec16<T>::n;i++)
+            xv[ u * Vec16<T>::n + i ] = lane<T>(t, i);
+      }
+      const T *blk = vp + (size_t)k * (B * B * 32);
+#pragma unroll
+      for(int i=0;i<B;i++)
+#pragma unroll
+         for(int j=0;j<B;j++)
+            y[i] += __ldg(blk + (i * B + j) * 32) * xv[j];
+   }
+}
+
+template<int B, int VS, class T>
+__global__ void __launch_bounds__(SV_THREADS)
+sv_spmv_dot_kernel(int nrow, const int64_t *__restrict__ soff, const int *__restrict__ deg,
+                   const int *__restrict__ col, const T *__restrict__ val,
+                   const T *__restrict__ p, T *__restrict__ q, double *part, GmdSvScal *sc)
+{
+   typedef typename Vec16<T>::type V;
+   constexpr int NV = VS / Vec16<T>::n;
+   double acc = 0., tot;
+   if(sv_stopped(sc))
+      return;
+   for(int r=blockIdx.x*blockDim.x+threadIdx.x;r<nrow;r+=gridDim.x*blockDim.x)
+   {
+      T y[VS];
+      sv_row_product<B, VS, T>(r, soff, deg, col, val, p, y);
+      V *qp = reinterpret_cast<V *>(q + (size_t)r * VS);
+      const V *pp = reinterpret_cast<const V *>(p + (size_t)r * VS);
+#pragma unroll
+      for(int u=0;u<NV;u++)
+      {
+         V t;
+#pragma unroll
+         for(int i=0;i<Vec16<T>::n;i++)
+            reinterpret_cast<T *>(&t)[i] = y[ u * Vec16<T>::n + i ];
+         qp[u] = t;
+         acc += dot16<T>(__ldg(pp + u), t);
+      }
+   }
+   if(sv_grid_sum(acc, part, sc, &tot))
+   {
+      sc->pq = tot;
+      if(tot > 0.)
+         sc->alpha = sc->rr / tot;
+      else
+      {
+         sc->alpha = 0.;
+         sc->done = 2;
+      }
+   }
+}
+
+template<class T>
+__global__ void __launch_bounds__(SV_THREADS)
+sv_update_kernel(size_t n, T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
+                 const T *__restrict__ q, double *part, GmdSvScal *sc)
+{
+   typedef typename Vec16<T>::type V;
+   const size_t nv = n / Vec16<T>::n;
+   double acc = 0., tot;
+   if(sv_stopped(sc))
+      return;
+   const T a = (T)sc->alpha;
+   V *xv = reinterpret_cast<V *>(x), *rv = reinterpret_cast<V *>(r);
+   const V *pv = reinterpret_cast<const V *>(p), *qv = reinterpret_cast<const V *>(q);
+   for(size_t i=(size_t)blockIdx.x*blockDim.x+threadIdx.x;i<nv;i+=(size_t)gridDim.x*blockDim.x)
+   {
+      V xx = xv[i], rr = rv[i];
+      const V pp = pv[i], qq = qv[i];
+#pragma unroll
+      for(int k=0;k<Vec16<T>::n;k++)
+      {
+         reinterpret_cast<T *>(&xx)[k] += a * lane<T>(pp, k);
+         reinterpret_cast<T *>(&rr)[k] -= a * lane<T>(qq, k);
+      }
+      xv[i] = xx;
+      rv[i] = rr;
+      acc += dot16<T>(rr, rr);
+   }
+   if(sv_grid_sum(acc, part, sc, &tot))
+   {
+      sc->beta = tot / sc->rr;
+      sc->rr = tot;
+      sc->it += 1;
+      if(tot <= sc->stop || sc->it >= sc->maxit)
+         sc->done = 1;
+   }
+}
+
+template<class T>
+__global__ void __launch_bounds__(SV_THREADS)
+sv_dir_kernel(size_t n, T *__restrict__ p, const T *__restrict__ r, const GmdSvScal *sc)
+{
+   typedef typename Vec16<T>::type V;
+   const size_t nv = n / Vec16<T>::n;
+   if(sv_stopped(sc))
+      return;
+   const T b = (T)sc->beta;
+   V *pv = reinterpret_cast<V *>(p);
+   const V *rv = reinterpret_cast<const V *>(r);
+   for(size_t i=(size_t)blockIdx.x*blockDim.x+threadIdx.x;i<nv;i+=(size_t)gridDim.x*blockDim.x)
+   {
+      V pp = pv[i];
+      const V rr = rv[i];
+#pragma unroll
+      for(int k=0;k<Vec16<T>::n;k++)
+         reinterpret_cast<T *>(&pp)[k] = lane<T>(rr, k) + b * lane<T>(pp, k);
+      pv[i] = pp;
+   }
+}
+
+template<int B, int VS>
+__global__ void __launch_bounds__(SV_THREADS)
+sv_residual_kernel(int nrow, const int64_t *__restrict__ soff, const int *__restrict__ deg,
+                   const int *__restrict__ col, const double *__restrict__ val,
+                   const double *__restrict__ b, const double *__restrict__ x,
+                   double *__restrict__ res, double *part, GmdSvScal *sc)
+{
+   double acc = 0., tot;
+   for(int r=blockIdx.x*blockDim.x+threadIdx.x;r<nrow;r+=gridDim.x*blockDim.x)
+   {
+      double y[VS];
+      sv_row_product<B, VS, double>(r, soff, deg, col, val, x, y);
+#pragma unroll
+      for(int i=0;i<VS;i++)
+      {
+         const double v = i < B ? __ldg(&b[ (size_t)r * VS + i ]) - y[i] : 0.;
+         res[ (size_t)r * VS + i ] = v;
+         acc += v * v;
+      }
+   }
+   if(sv_grid_sum(acc, part, sc, &tot))
+      sc->rt = tot;
+}
+
+__global__ void __launch_bounds__(SV_THREADS)
+sv_ir_begin_kernel(size_t n, const double *__restrict__ r64, float *__restrict__ r32,
+                   float *__restrict__ p32, float *__restrict__ d32, double *part,
+                   GmdSvScal *sc, double tin2, int maxit)
+{
+   double acc = 0., tot;
+   const double rt = sc->rt;
+   const double s = rt > 0. ? 1.0 / sqrt(rt) : 0.;
+   for(size_t i=(size_t)blockIdx.x*blockDim.x+threadIdx.x;i<n;i+=(size_t)gridDim.x*blockDim.x)
+   {
+      const float v = (float)(r64[i] * s);
+      r32[i] = v;
+      p32[i] = v;
+      d32[i] = 0.f;
+      acc += (double)v * (double)v;
+   }
+   if(sv_grid_sum(acc, part, sc, &tot))
+   {
+      sc->rr = tot;
+      sc->stop = tin2 * tot;
+      sc->it = 0;
+      sc->maxit = maxit;
+      sc->done = tot > 0. ? 0 : 1;
+   }
+}
+
+__global__ void __launch_bounds__(SV_THREADS)
+sv_ir_end_kernel(size_t n, double *__restrict__ x64, const float *__restrict__ d32,
+                 const GmdSvScal *sc)
+{
+   const double s = sqrt(sc->rt);
+   for(size_t i=(size_t)blockIdx.x*blockDim.x+threadIdx.x;i<n;i+=(size_t)gridDim.x*blockDim.x)
+      x64[i] += s * (double)d32[i];
+}
+
+__global__ void __launch_bounds__(SV_THREADS)
+sv_to_f32_kernel(const double *__restrict__ src, float *__restrict__ dst, size_t n)
+{
+   for(size_t i=(size_t)blockIdx.x*blockDim.x+threadIdx.x;i<n;i+=(size_t)gridDim.x*blockDim.x)
+      dst[i] = (float)src[i];
+}
+
+/* ------------------------------------------------------------------------- */
+/* host wrappers                                                              */
+/* ------------------------------------------------------------------------- */
+
+static int sv_ok(void)
+{
+   return cudaGetLastError() == cudaSuccess;
+}
+
+/* flat kernels: 8 blocks per SM, grid-stride */
+static unsigned sv_flat_grid(GmdCtx *ctx, size_t n)
+{
+   size_t g = (n + SV_THREADS - 1) / SV_THREADS, cap = 8 * (size_t)gmd_num_sms(ctx);
+   if(g > cap) g = cap;
+   if(g > GMD_SV_MAXBLK) g = GMD_SV_MAXBLK;
+   return (unsigned)(g ? g : 1);
+}
+
+/* row kernels: one thread per block row */
+static unsigned sv_row_grid(int nrow)
+{
+   long long g = ((long long)nrow + SV_THREADS - 1) / SV_THREADS;
+   if(g > GMD_SV_MAXBLK) g = GMD_SV_MAXBLK;
+   return (unsigned)(g < 1 ? 1 : g);
+}
+
+extern "C" int gmd_sv_lanes(int B)
+{
+   return B <= 4 ? 4 : 8;
+}
+
+extern "C" int gmd_sv_init(GmdCtx *ctx, size_t n, int B, const double *bsrc, double *b64,
+                           void *x, void *r, void *p, int fltsiz, double *part, GmdSvScal *sc,
+                           double tol2, int maxit)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   const unsigned g = sv_flat_grid(ctx, n);
+   const int vs = gmd_sv_lanes(B);
+   if(fltsiz == 8)
+      sv_init_kernel<double><<<g, SV_THREADS, 0, st>>>(n, B, vs, bsrc, b64, (double *)x,
+         (double *)r, (double *)p, part, sc, tol2, maxit);
+   else
+      sv_init_kernel<float><<<g, SV_THREADS, 0, st>>>(n, B, vs, bsrc, b64, (float *)x,
+         (float *)r, (float *)p, part, sc, tol2, maxit);
+   return sv_ok();
+}
+
+template<int B, int VS, class T>
+static void sv_spmv_launch(cudaStream_t st, const GmlSellDev *A, const void *p, void *q,
+                           double *part, GmdSvScal *sc)
+{
+   sv_spmv_dot_kernel<B, VS, T><<<sv_row_grid(A->NmbLin), SV_THREADS, 0, st>>>(A->NmbLin,
+      A->SlcOff, A->Deg, A->Col, (const T *)A->Val, (const T *)p, (T *)q, part, sc);
+}
+
+template<class T>
+static int sv_spmv_t(cudaStream_t st, const GmlSellDev *A, const void *p, void *q,
+                     double *part, GmdSvScal *sc)
+{
+   switch(A->BlkSiz)
+   {
+      case 3: sv_spmv_launch<3, 4, T>(st, A, p, q, part, sc); break;
+      case 4: sv_spmv_launch<4, 4, T>(st, A, p, q, part, sc); break;
+      case 5: sv_spmv_launch<5, 8, T>(st, A, p, q, part, sc); break;
+      case 7: sv_spmv_launch<7, 8, T>(st, A, p, q, part, sc); break;
+      default: return 0;
+   }
+   return sv_ok();
+}
+
+extern "C" int gmd_sv_spmv_dot(GmdCtx *ctx, const GmlSellDev *A, const void *p, void *q,
+                               double *part, GmdSvScal *sc)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   return A->FltSiz == 8 ? sv_spmv_t<double>(st, A, p, q, part, sc)
+                         : sv_spmv_t<float>(st, A, p, q, part, sc);
+}
+
+extern "C" int gmd_sv_update(GmdCtx *ctx, int fltsiz, size_t n, void *x, void *r,
+                             const void *p, const void *q, double *part, GmdSvScal *sc)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   if(fltsiz == 8)
+      sv_update_kernel<double><<<sv_flat_grid(ctx, n / 2), SV_THREADS, 0, st>>>(n, (double *)x,
+         (double *)r, (const double *)p, (const double *)q, part, sc);
+   else
+      sv_update_kernel<float><<<sv_flat_grid(ctx, n / 4), SV_THREADS, 0, st>>>(n, (float *)x,
+         (float *)r, (const float *)p, (const float *)q, part, sc);
+   return sv_ok();
+}
+
+extern "C" int gmd_sv_dir(GmdCtx *ctx, int fltsiz, size_t n, void *p, const void *r,
+                          GmdSvScal *sc)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   if(fltsiz == 8)
+      sv_dir_kernel<double><<<sv_flat_grid(ctx, n / 2), SV_THREADS, 0, st>>>(n, (double *)p,
+         (const double *)r, sc);
+   else
+      sv_dir_kernel<float><<<sv_flat_grid(ctx, n / 4), SV_THREADS, 0, st>>>(n, (float *)p,
+         (const float *)r, sc);
+   return sv_ok();
+}
+
+extern "C" int gmd_sv_residual(GmdCtx *ctx, const GmlSellDev *A, const double *b,
+                               const double *x, double *r, double *part, GmdSvScal *sc)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   const double *val = (const double *)A->Val;
+   const unsigned g = sv_row_grid(A->NmbLin);
+   if(A->FltSiz != 8)
+      return 0;
+   switch(A->BlkSiz)
+   {
+      case 3: sv_residual_kernel<3, 4><<<g, SV_THREADS, 0, st>>>(A->NmbLin, A->SlcOff, A->Deg,
+                 A->Col, val, b, x, r, part, sc); break;
+      case 4: sv_residual_kernel<4, 4><<<g, SV_THREADS, 0, st>>>(A->NmbLin, A->SlcOff, A->Deg,
+                 A->Col, val, b, x, r, part, sc); break;
+      case 5: sv_residual_kernel<5, 8><<<g, SV_THREADS, 0, st>>>(A->NmbLin, A->SlcOff, A->Deg,
+                 A->Col, val, b, x, r, part, sc); break;
+      case 7: sv_residual_kernel<7, 8><<<g, SV_THREADS, 0, st>>>(A->NmbLin, A->SlcOff, A->Deg,
+                 A->Col, val, b, x, r, part, sc); break;
+      default: return 0;
+   }
+   return sv_ok();
+}
+
+extern "C" int gmd_sv_ir_begin(GmdCtx *ctx, size_t n, const double *r64, float *r32, float *p32,
+                               float *d32, double *part, GmdSvScal *sc, double tin2, int maxit)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   sv_ir_begin_kernel<<<sv_flat_grid(ctx, n), SV_THREADS, 0, st>>>(n, r64, r32, p32, d32, part,
+      sc, tin2, maxit);
+   return sv_ok();
+}
+
+extern "C" int gmd_sv_ir_end(GmdCtx *ctx, size_t n, double *x64, const float *d32, GmdSvScal *sc)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   sv_ir_end_kernel<<<sv_flat_grid(ctx, n), SV_THREADS, 0, st>>>(n, x64, d32, sc);
+   return sv_ok();
+}
+
+extern "C" int gmd_sv_to_f32(GmdCtx *ctx, const double *src, float *dst, size_t n)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   sv_to_f32_kernel<<<sv_flat_grid(ctx, n), SV_THREADS, 0, st>>>(src, dst, n);
+   return sv_ok();
+}

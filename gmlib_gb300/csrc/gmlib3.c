@@ -276,6 +276,7 @@ void GmlStop(size_t GmlIdx)
       if(gml->dat[i].use)
          release_data(gml, &gml->dat[i]);
 
+   gml_release_solvers(gml);
    gml_release_matrices(gml);
 
    for(i=1;i<=gml->NmbKrn && i<=GmlMaxKrn;i++)

@@ -92,6 +92,11 @@ int      GmlxCompileKernelV   (size_t, const char *src, const char *name, int Ms
 int      GmlxSetData          (size_t, int DatIdx, const void *buf, size_t bytes);
 int      GmlxGetData          (size_t, int DatIdx, void *buf, size_t bytes);
 
+/* Datatype index holding the lines of a GmlNewVector vector (padded lines
+   of the vector's lane count), for GmlxGetData / GmlxSetData.  Extends
+   GmlNewVector (gmlib3.c:1434-1560), which keeps that index private. */
+int      GmlxVectorData       (size_t, int VecIdx);
+
 /* Size in bytes, number of lines and device address of a datatype. */
 size_t   GmlxDataBytes        (size_t, int DatIdx);
 int      GmlxDataLines        (size_t, int DatIdx);
@@ -198,6 +203,143 @@ int      GmlxSmoothQualityLoop(size_t, int nsweeps, float omega, double h, GmlxQ
 /* Algorithmic (unique) bytes of one sweep and of one quality pass for the
    current mesh, the numerators of the roofline figures. */
 int      GmlxMeshBytes        (size_t, double *sweep_bytes, double *quality_bytes);
+
+/* ---------------------------------------------------------------------------
+ * Batched meshes: many tetrahedral meshes of uneven size in one instance,
+ * smoothed and measured together.  No counterpart in the reference (one
+ * mesh per instance, one launch per kernel call, gmlib3.c:3064-3222).
+ * ------------------------------------------------------------------------- */
+
+enum GmlxBatchMode { GmlxBatchQueue = 0, GmlxBatchLoop = 1 };
+
+/* Declare NmbMsh meshes (vertex and tet counts, edge length h of each for
+   the FP64 determinant threshold 1e-6 h^3).  Creates the instance's vertex
+   and tetrahedron datatypes holding all meshes packed (each mesh's vertices
+   start on a multiple of 256); the instance must not have them yet. */
+int      GmlxBatchCreate      (size_t, int NmbMsh, const int *NmbVer, const int *NmbTet,
+                               const double *h);
+
+/* Mesh MshIdx (0-based): crd 4 floats per vertex, ref one int per vertex
+   (NULL: 0), tet 4 local vertex indices per tet. */
+int      GmlxBatchSetMesh     (size_t, int MshIdx, const float *crd, const int *ref,
+                               const int *tet);
+
+/* Upload the packed meshes and build their topology (GmlxMeshSetup on the
+   packed mesh, fix as there). */
+int      GmlxBatchSetup       (size_t, int fix);
+
+/* nsweeps Jacobi sweeps then the quality statistics of every mesh.
+   GmlxBatchQueue: one persistent launch drains a (mesh, range) tile queue,
+   captured once as a CUDA graph and replayed; GmlxBatchLoop: the per-mesh
+   launch loop.  res (may be NULL) receives NmbMsh results, tet indices local
+   to each mesh.  The coordinates are updated in place. */
+int      GmlxBatchRun         (size_t, int nsweeps, float omega, int mode, GmlxQuality *res);
+
+/* Coordinates (4 floats per vertex) and inverted-element flags of a mesh. */
+int      GmlxBatchGetMesh     (size_t, int MshIdx, float *crd);
+int      GmlxBatchFlags       (size_t, int MshIdx, unsigned *flags, size_t nwords);
+
+/* Time the queue on the packed meshes with several tile and grid sizes and
+   keep the fastest (the coordinates are restored afterwards); read back
+   the choice and the tile count. */
+int      GmlxBatchTune        (size_t, int nsweeps, float omega);
+int      GmlxBatchInfo        (size_t, int *TileSlices, int *TileTets, int *grid, int *ntile);
+
+/* ---------------------------------------------------------------------------
+ * Request loop: quality, smoothing and solve requests on registered meshes
+ * and systems, served from one GPU with continuous batching against a
+ * device-memory budget.  No counterpart in the reference.
+ * ------------------------------------------------------------------------- */
+
+enum GmlxReqKind   { GmlxReqQuality = 0, GmlxReqSmooth = 1, GmlxReqSolve = 2 };
+enum GmlxServeMode { GmlxServeBatching = 0, GmlxServeSerial = 1 };
+
+typedef struct
+{
+   int      kind, target;       /* GmlxReqKind; index from GmlxServeAdd* */
+   double   arrival;            /* seconds from the start of the run, non-decreasing */
+   double   start, finish;      /* filled in: seconds from the start of the run */
+   int      status;             /* filled in: 1 done, 0 failed */
+   int      NmbIte;             /* solve: CG iterations */
+   double   RelRes;             /* solve: |b - A x| / |b| */
+   GmlxQuality qal;             /* quality, or quality after the 10th smoothing sweep */
+}GmlxRequest;
+
+typedef struct
+{
+   int      completed, failed, loads, evictions;
+   double   seconds, throughput, mean, p50, p99, max, peak_bytes;
+}GmlxServeStats;
+
+/* Server on device dev with a device-memory budget (bytes) for resident
+   targets and NmbSlot concurrent requests (1..64). */
+size_t   GmlxServeNew         (int dev, double BudgetBytes, int NmbSlot);
+
+/* Register a tet mesh (crd 4 floats per vertex, ref per vertex or NULL;
+   vertices with a non-zero ref stay fixed when smoothing; h for the FP64
+   determinant threshold) or a 3x3-block SPD system (CSR as GmlNewMatrix,
+   FP64 values, rhs 3 per row).  The arrays are used in place and must
+   outlive the server.  Returns the target index, or -1. */
+int      GmlxServeAddMesh     (size_t srv, int NmbVer, const float *crd, const int *ref,
+                               int NmbTet, const int *tet, double h);
+int      GmlxServeAddSystem   (size_t srv, int NmbLin, int NmbBlk, const int *lin,
+                               const int *col, const double *val, const double *rhs);
+
+/* Serve NmbReq requests arriving at their times.  GmlxReqQuality: mean-ratio
+   statistics; GmlxReqSmooth: 10 sweeps (omega 1) each followed by the
+   statistics, the mesh's registered coordinates restored afterwards;
+   GmlxReqSolve: FP32 CG in FP64 refinement to 1e-10.  GmlxServeBatching:
+   continuous batching over NmbSlot slots with resident targets;
+   GmlxServeSerial: one request at a time, each on a fresh instance.
+   Returns 1 when the loop ran (individual failures are in status). */
+int      GmlxServeRun         (size_t srv, GmlxRequest *req, int NmbReq, int mode,
+                               GmlxServeStats *st);
+
+/* Estimated device bytes of a target when resident (what admission
+   charges against the budget); number of resident targets and their bytes. */
+double   GmlxServeTargetBytes (size_t srv, int target);
+int      GmlxServeResident    (size_t srv, double *bytes);
+void     GmlxServeFree        (size_t srv);
+
+/* ---------------------------------------------------------------------------
+ * Conjugate gradients on a GmlNewMatrix block matrix.  No counterpart in the
+ * reference: its LinearSolver example runs a fixed-point loop with
+ * GmlMultMatVec / GmlMultDiagMatVec / GmlAddVec3
+ * (examples/LinearSolver/LinearSolver.c:300-338).
+ * ------------------------------------------------------------------------- */
+
+enum GmlxCgMode { GmlxCgFp64 = 0, GmlxCgMixed = 1 };
+
+typedef struct
+{
+   int      NmbIte;        /* CG iterations (FP32 iterations in GmlxCgMixed) */
+   int      NmbOut;        /* refinement steps (1 for GmlxCgFp64) */
+   double   RelRes;        /* |b - A x| / |b|, recomputed in FP64 at the end */
+   double   Seconds;       /* device time of the solve (CUDA events) */
+}GmlxSolveInfo;
+
+/* Solve A x = b for a symmetric positive definite matrix MatIdx (GmlDbl,
+   diagonal blocks stored in the matrix), RhsIdx and SolIdx being GmlDbl
+   vectors of the matrix's size and block size.  x starts at 0.
+   GmlxCgFp64: CG in FP64.  GmlxCgMixed: CG in FP32 (FP32 copy of the matrix,
+   FP32 vectors, FP64 dot products) inside FP64 iterative refinement with
+   the true residual b - A x in FP64.  Stops when |b - A x| <= tol |b| or after
+   MaxIte CG iterations.  Returns 1 when converged, 0 when not, negative on
+   errors (-1 matrix, -2 vectors, -3 types or sizes, -4 arguments, -5 memory,
+   -6 device, -7 breakdown: p.Ap <= 0). */
+int      GmlxSolveCG          (size_t, int MatIdx, int RhsIdx, int SolIdx, int mode,
+                               double tol, int MaxIte, GmlxSolveInfo *info);
+
+/* Symmetric positive definite 3x3-block system on the vertex graph of the
+   n^3-hex cube of GmlxCubeMesh (no jitter, Hilbert order): row v holds v and
+   the vertices sharing a tet with v, columns ascending; off-diagonal block
+   entries uniform in [-1, 0] from the seed, A_ji = A_ij^T; diagonal block
+   diag(1 + sum of |off-diagonal entries| of each scalar row); rhs uniform in
+   [-1, 1].  lin has NmbLin + 1 entries, col NmbBlk, val 9 NmbBlk (row-major
+   blocks), rhs 3 NmbLin (may be NULL).  Returns 1, or 0 on bad sizes. */
+int      GmlxCubeSpdSizes     (int n, int split, int *NmbLin, int *NmbBlk);
+int      GmlxCubeSpdMatrix    (int n, int split, uint64_t seed, int *lin, int *col,
+                               double *val, double *rhs);
 
 /* ---------------------------------------------------------------------------
  * Synthetic meshes and renumbering (host utilities).  No counterpart in the

@@ -35,6 +35,9 @@ def lib():
         _c.orc_det1.restype = ctypes.c_double
         _c.orc_reduce.restype = ctypes.c_double
         _c.orc_reduce.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        _c.orc_rel_residual.restype = ctypes.c_double
+        _c.orc_cg.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5 + \
+            [ctypes.c_double, ctypes.c_int]
     return _c
 
 
@@ -215,3 +218,42 @@ def quality_stats(crd, tet):
     lib().orc_quality_stats(nt, _ptr(crd), _ptr(tet), _ptr(q), _ptr(hist), _ptr(flags),
                             ctypes.byref(ninv))
     return q, hist, flags, ninv.value
+
+
+# ------------------------------------------------------------ block algebra
+
+def _bsr_args(lin, col, val):
+    lin = np.ascontiguousarray(lin, np.int32)
+    col = np.ascontiguousarray(col, np.int32)
+    val = np.ascontiguousarray(val, np.float64)
+    b = val.shape[-1]
+    return lin, col, val, b
+
+
+def bsr_spmv(lin, col, val, x):
+    """y = A x (FP64, long-double accumulation); val is [nnzb, b, b]."""
+    lin, col, val, b = _bsr_args(lin, col, val)
+    nrow = len(lin) - 1
+    x = np.ascontiguousarray(x, np.float64).reshape(nrow, b)
+    y = np.zeros((nrow, b), np.float64)
+    lib().orc_bsr_spmv(nrow, b, _ptr(lin), _ptr(col), _ptr(val), _ptr(x), _ptr(y))
+    return y
+
+
+def rel_residual(lin, col, val, rhs, x):
+    lin, col, val, b = _bsr_args(lin, col, val)
+    nrow = len(lin) - 1
+    rhs = np.ascontiguousarray(rhs, np.float64)
+    x = np.ascontiguousarray(x, np.float64)
+    return lib().orc_rel_residual(nrow, b, _ptr(lin), _ptr(col), _ptr(val), _ptr(rhs), _ptr(x))
+
+
+def cg(lin, col, val, rhs, tol, maxit):
+    """FP64 CG from x = 0; returns (x, iterations)."""
+    lin, col, val, b = _bsr_args(lin, col, val)
+    nrow = len(lin) - 1
+    rhs = np.ascontiguousarray(rhs, np.float64)
+    x = np.zeros((nrow, b), np.float64)
+    it = lib().orc_cg(nrow, b, _ptr(lin), _ptr(col), _ptr(val), _ptr(rhs), _ptr(x),
+                      float(tol), int(maxit))
+    return x, it

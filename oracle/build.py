@@ -34,7 +34,7 @@ def _run(cmd):
 
 
 def build_oracle(force=False):
-    names = ("oracle.c", "oracle_mesh.c", "baseline.c")
+    names = ("oracle.c", "oracle_mesh.c", "oracle_linalg.c", "baseline.c")
     srcs = [os.path.join(HERE, f) for f in names + ("oracle.h",)]
     if force or _stale(LIB, srcs):
         _run(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-std=gnu11"]

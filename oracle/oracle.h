@@ -31,6 +31,14 @@ void   orc_laplace(int nv, double *crd, const long long *ptr, const int *col, do
 void   orc_quality_stats(int nt, const float *crd, const int *tet, double *q, unsigned *hist,
                          unsigned *flags, unsigned *ninv);
 
+/* oracle_linalg.c */
+void   orc_bsr_spmv(int nrow, int b, const int *lin, const int *col, const double *val,
+                    const double *x, double *y);
+double orc_rel_residual(int nrow, int b, const int *lin, const int *col, const double *val,
+                        const double *rhs, const double *x);
+int    orc_cg(int nrow, int b, const int *lin, const int *col, const double *val,
+              const double *rhs, double *x, double tol, int maxit);
+
 #ifdef __cplusplus
 }
 #endif
