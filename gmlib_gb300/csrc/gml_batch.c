@@ -392,7 +392,7 @@ static int bat_loop_work(GmlSct *gml, BatSct *b, NatSct *n, int nsweeps, float o
          t = in; in = out; out = t;
       }
       if(!gmd_mesh_quality(gml->dev, x->nt, (const int *)td->GpuMem + 4 * (size_t)x->t0, fin,
-                           x->thr, NULL, b->flags + x->f0, b->stats + m, n->err))
+                           x->thr, NULL, b->flags + x->f0, b->stats + m, n->err, 0))
          return 0;
    }
    return !(nsweeps & 1) || gmd_d2d_async(gml->dev, vd->GpuMem, n->crd2, (size_t)b->nv * 16);

@@ -76,6 +76,10 @@ int      gmd_reduce_f32(GmdCtx *ctx, int op, const float *in, int n, double *res
                         void *scratch);
 size_t   gmd_reduce_scratch_bytes(int n);
 
+/* exclusive prefix sums: out[0..n-1] and the total in out[n] (gml_scan.cu) */
+int      gmd_scan_excl_i32(GmdCtx *ctx, const int *in, int *out, int n);
+int      gmd_scan_excl_i64(GmdCtx *ctx, const long long *in, long long *out, int n);
+
 /* min/argmin/max/argmax of a float field, smallest index wins ties. */
 int      gmd_minmax_arg_f32(GmdCtx *ctx, const float *in, int n,
                             float *vmin, int *imin, float *vmax, int *imax,

@@ -113,6 +113,7 @@ typedef struct
    int         TimOff;                /* 1: no per-launch timing events */
    int         Offline;               /* 1: no GPU, code generation only */
    int         Quiet;                 /* 1: no informational messages */
+   int         PinOff;                /* 1: pageable host mirrors (no page locking) */
    char        **Names;               /* interned strings owned by the instance */
    int         NmbNames, CapNames;
    void        *ext;                  /* state of the native extensions */

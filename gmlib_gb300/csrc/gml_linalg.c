@@ -77,96 +77,6 @@ static void vec_lanes(int BlkSiz, int *NmbValTyp, int *VecValSiz)
    else                  { *NmbValTyp = 4; *VecValSiz = 16; }
 }
 
-int gml_sell_build(int NmbLin, int BlkSiz, int FltSiz, const void *val,
-                   const int *col, const int *lin, GmlSell *s)
-{
-   int nsl = (NmbLin + 31) / 32, sl, r, k, c, bb = BlkSiz * BlkSiz;
-   size_t tot = 0;
-
-   memset(s, 0, sizeof(GmlSell));
-   s->NmbLin = NmbLin;
-   s->BlkSiz = BlkSiz;
-   s->FltSiz = FltSiz;
-   s->NmbSlc = nsl;
-   s->SlcOff = malloc((size_t)(nsl + 1) * sizeof(int64_t));
-   s->Deg    = malloc((size_t)NmbLin * sizeof(int));
-   if(!s->SlcOff || !s->Deg)
-      return 0;
-
-   for(sl=0;sl<nsl;sl++)
-   {
-      int w = 0;
-      s->SlcOff[sl] = (int64_t)tot;
-      for(r=sl*32;r<sl*32+32 && r<NmbLin;r++)
-      {
-         int d = lin[r+1] - lin[r];
-         s->Deg[r] = d;
-         if(d > w) w = d;
-      }
-      tot += (size_t)w;
-   }
-   s->SlcOff[nsl] = (int64_t)tot;
-   s->NmbCol = tot;
-
-   s->Col = calloc(tot * 32, sizeof(int));
-   s->Val = calloc(tot * 32 * (size_t)bb, FltSiz);
-   if(!s->Col || !s->Val)
-      return 0;
-
-   for(sl=0;sl<nsl;sl++)
-      for(r=sl*32;r<sl*32+32 && r<NmbLin;r++)
-      {
-         int lane = r & 31;
-         for(k=0;k<s->Deg[r];k++)
-         {
-            size_t e = (size_t)(s->SlcOff[sl] + k);
-            size_t src = (size_t)lin[r] + k;
-            s->Col[ e * 32 + lane ] = col[ src ];
-            for(c=0;c<bb;c++)
-            {
-               size_t dst = (e * bb + c) * 32 + lane;
-               if(FltSiz == 4)
-                  ((float *)s->Val)[dst] = ((const float *)val)[ src * bb + c ];
-               else
-                  ((double *)s->Val)[dst] = ((const double *)val)[ src * bb + c ];
-            }
-         }
-      }
-
-   return 1;
-}
-
-void gml_sell_free(GmlSell *s)
-{
-   free(s->SlcOff); free(s->Deg); free(s->Col); free(s->Val);
-   memset(s, 0, sizeof(GmlSell));
-}
-
-int gml_sell_upload(GmlSct *gml, const GmlSell *s, GmlSellDev *d)
-{
-   size_t bb = (size_t)s->BlkSiz * s->BlkSiz;
-   memset(d, 0, sizeof(GmlSellDev));
-   d->NmbLin = s->NmbLin;
-   d->BlkSiz = s->BlkSiz;
-   d->FltSiz = s->FltSiz;
-   d->NmbSlc = s->NmbSlc;
-   d->NmbCol = s->NmbCol;
-   d->bytes  = (size_t)(s->NmbSlc + 1) * 8 + (size_t)s->NmbLin * 4
-             + s->NmbCol * 32 * 4 + s->NmbCol * 32 * bb * s->FltSiz;
-   d->SlcOff = gmd_alloc(gml->dev, (size_t)(s->NmbSlc + 1) * 8);
-   d->Deg    = gmd_alloc(gml->dev, (size_t)s->NmbLin * 4);
-   d->Col    = gmd_alloc(gml->dev, s->NmbCol * 32 * 4);
-   d->Val    = gmd_alloc(gml->dev, s->NmbCol * 32 * bb * s->FltSiz);
-   if(!d->SlcOff || !d->Deg || !d->Col || !d->Val)
-      return 0;
-   gmd_h2d_async(gml->dev, d->SlcOff, s->SlcOff, (size_t)(s->NmbSlc + 1) * 8);
-   gmd_h2d_async(gml->dev, d->Deg, s->Deg, (size_t)s->NmbLin * 4);
-   gmd_h2d_async(gml->dev, d->Col, s->Col, s->NmbCol * 32 * 4);
-   gmd_h2d_async(gml->dev, d->Val, s->Val, s->NmbCol * 32 * bb * s->FltSiz);
-   /* the host arrays are pageable: the copies are staged before return */
-   return gmd_sync(gml->dev);
-}
-
 void gml_sell_dev_free(GmlSct *gml, GmlSellDev *d)
 {
    gmd_free(gml->dev, d->SlcOff);
@@ -174,6 +84,76 @@ void gml_sell_dev_free(GmlSct *gml, GmlSellDev *d)
    gmd_free(gml->dev, d->Col);
    gmd_free(gml->dev, d->Val);
    memset(d, 0, sizeof(GmlSellDev));
+}
+
+/* SELL-32 image built on the device from the caller's CSR arrays: they are
+   uploaded once, the slice widths and offsets are computed and scanned on
+   the device, and a fill kernel scatters the blocks.  Returns 1, or 0 with
+   a message (bad row pointers or columns, no memory). */
+static int sell_build_device(GmlSct *gml, int NmbLin, int NmbBlk, int BlkSiz, int FltSiz,
+                             const void *val, const int *col, const int *lin, GmlSellDev *d)
+{
+   const size_t bb = (size_t)BlkSiz * BlkSiz;
+   const int nsl = (NmbLin + 31) / 32;
+   int *dlin, *dcol, *err, herr = 0, ok = 0;
+   void *dval;
+   long long *width, tot = 0;
+
+   memset(d, 0, sizeof(GmlSellDev));
+   d->NmbLin = NmbLin;
+   d->BlkSiz = BlkSiz;
+   d->FltSiz = FltSiz;
+   d->NmbSlc = nsl;
+   dlin = gmd_alloc(gml->dev, (size_t)(NmbLin + 1) * 4);
+   dcol = gmd_alloc(gml->dev, (size_t)NmbBlk * 4);
+   dval = gmd_alloc(gml->dev, (size_t)NmbBlk * bb * FltSiz);
+   err = gmd_alloc(gml->dev, sizeof(int));
+   width = gmd_alloc(gml->dev, (size_t)(nsl + 1) * 8);
+   d->Deg = gmd_alloc(gml->dev, (size_t)NmbLin * 4);
+   d->SlcOff = gmd_alloc(gml->dev, (size_t)(nsl + 1) * 8);
+   if(!dlin || !dcol || !dval || !err || !width || !d->Deg || !d->SlcOff)
+      goto done;
+   /* the caller's arrays are pageable: each copy is staged before it returns */
+   if(!gmd_h2d_async(gml->dev, dlin, lin, (size_t)(NmbLin + 1) * 4)
+   || !gmd_h2d_async(gml->dev, dcol, col, (size_t)NmbBlk * 4)
+   || !gmd_h2d_async(gml->dev, dval, val, (size_t)NmbBlk * bb * FltSiz)
+   || !gmd_sell_widths(gml->dev, NmbLin, dlin, d->Deg, width, err)
+   || !gmd_scan_excl_i64(gml->dev, width, (long long *)d->SlcOff, nsl)
+   || !gmd_d2h(gml->dev, &tot, (long long *)d->SlcOff + nsl, sizeof(long long))
+   || !gmd_d2h(gml->dev, &herr, err, sizeof(int)))
+      goto done;
+   if(herr)
+   {
+      printf("GmlNewMatrix: row pointers decrease\n");
+      goto done;
+   }
+   d->NmbCol = (size_t)tot;
+   d->Col = gmd_alloc(gml->dev, (size_t)tot * 32 * 4);
+   d->Val = gmd_alloc(gml->dev, (size_t)tot * 32 * bb * FltSiz);
+   if(!d->Col || !d->Val)
+      goto done;
+   if(!gmd_sell_fill(gml->dev, NmbLin, (int)bb, FltSiz, dlin, dcol, dval,
+                     (const long long *)d->SlcOff, d->Col,
+                     d->Val, err)
+   || !gmd_d2h(gml->dev, &herr, err, sizeof(int)))
+      goto done;
+   if(herr)
+   {
+      printf("GmlNewMatrix: column index out of range\n");
+      goto done;
+   }
+   d->bytes = (size_t)(nsl + 1) * 8 + (size_t)NmbLin * 4 + (size_t)tot * 32 * 4
+            + (size_t)tot * 32 * bb * FltSiz;
+   ok = 1;
+done:
+   gmd_free(gml->dev, dlin);
+   gmd_free(gml->dev, dcol);
+   gmd_free(gml->dev, dval);
+   gmd_free(gml->dev, err);
+   gmd_free(gml->dev, width);
+   if(!ok)
+      gml_sell_dev_free(gml, d);
+   return ok;
 }
 
 /* ========================================================================= */
@@ -186,7 +166,6 @@ int GmlNewMatrix(size_t GmlIdx, int NmbLin, int NmbBlk, int BlkSiz, void *val,
    GETGMLPTR(gml, GmlIdx);
    int MatIdx, FltSiz;
    GmlMatSct *mat;
-   GmlSell sell;
    GmlSellDev *dev;
 
    if(NmbLin < 1 || NmbBlk < 1 || BlkSiz < 1 || BlkSiz > 10)
@@ -195,7 +174,9 @@ int GmlNewMatrix(size_t GmlIdx, int NmbLin, int NmbBlk, int BlkSiz, void *val,
       return 0;
    if(FltTyp != GmlFlt && FltTyp != GmlDbl)
       return 0;
-   if(!val || !col || !lin || lin[NmbLin] - lin[0] != NmbBlk)
+   /* row pointers start at 0 and end at NmbBlk; the device build checks
+      that they never decrease and that every column is a row index */
+   if(!val || !col || !lin || lin[0] != 0 || lin[NmbLin] != NmbBlk)
       return 0;
    if(!(MatIdx = get_mat_idx(gml)))
       return 0;
@@ -207,18 +188,10 @@ int GmlNewMatrix(size_t GmlIdx, int NmbLin, int NmbBlk, int BlkSiz, void *val,
    mat->BlkSiz = BlkSiz;
    mat->FltTyp = FltTyp;
 
-   if(!gml_sell_build(NmbLin, BlkSiz, FltSiz, val, col, lin, &sell))
-   {
-      gml_sell_free(&sell);
-      mat->use = 0;
-      return 0;
-   }
-
    dev = calloc(1, sizeof(GmlSellDev));
-   if(!dev || !gml_sell_upload(gml, &sell, dev))
+   if(!dev || !sell_build_device(gml, NmbLin, NmbBlk, BlkSiz, FltSiz, val, col, lin, dev))
    {
-      printf("Cannot allocate the sparse matrix on the GPU\n");
-      gml_sell_free(&sell);
+      printf("Cannot build the sparse matrix on the GPU\n");
       free(dev);
       mat->use = 0;
       return 0;
@@ -226,12 +199,11 @@ int GmlNewMatrix(size_t GmlIdx, int NmbLin, int NmbBlk, int BlkSiz, void *val,
 
    if(!gml->Quiet)
    {
-      printf(" Matrix slices = %d (SELL-32)\n", sell.NmbSlc);
+      printf(" Matrix slices = %d (SELL-32)\n", dev->NmbSlc);
       printf("  sparse nnz = %d, vectorized nnz = %zu, occupency = %.1f%%\n",
-             NmbBlk, sell.NmbCol * 32, (100. * NmbBlk) / (double)(sell.NmbCol * 32));
+             NmbBlk, dev->NmbCol * 32, (100. * NmbBlk) / (double)(dev->NmbCol * 32));
    }
 
-   gml_sell_free(&sell);
    mat->Val = dev;
    gml->MemSiz += dev->bytes;
    mat->KrnIdx = gml_new_kernel_slot(gml, GmlKrnMatVec, "MulMatVecSell");

@@ -13,20 +13,11 @@
 extern "C" {
 #endif
 
-/* host-side SELL-32 image of a block CSR matrix:
-   entry k of row r (slice s = r/32, lane = r%32) has its column at
+/* SELL-32 image of a block CSR matrix on the device: entry k of row r
+   (slice s = r/32, lane = r%32) has its column at
    Col[(SlcOff[s] + k) * 32 + lane] and block value c (row-major b x b) at
-   Val[((SlcOff[s] + k) * b*b + c) * 32 + lane]. */
-typedef struct
-{
-   int      NmbLin, BlkSiz, FltSiz, NmbSlc;
-   size_t   NmbCol;          /* sum of slice widths */
-   int64_t  *SlcOff;
-   int      *Deg, *Col;
-   void     *Val;
-}GmlSell;
-
-/* device copy */
+   Val[((SlcOff[s] + k) * b*b + c) * 32 + lane]; Deg[r] is the row's block
+   count and padding entries hold column 0 and zero values. */
 typedef struct
 {
    int      NmbLin, BlkSiz, FltSiz, NmbSlc;
@@ -47,6 +38,13 @@ int gmd_vec_add3(struct GmdCtx *ctx, const void *u, const void *v, const void *w
 int gmd_vec_scale(struct GmdCtx *ctx, void *u, size_t n, int fltsiz, double s);
 int gmd_vec_rownorm(struct GmdCtx *ctx, const void *u, int us, int nlanes, int fltsiz,
                     int nlin, float *out);
+/* device SELL-32 repack: row degrees and slice widths, then the fill;
+   err bit 1: decreasing row pointers, bit 2: column out of range */
+int gmd_sell_widths(struct GmdCtx *ctx, int nrow, const int *lin, int *deg, long long *width,
+                    int *err);
+int gmd_sell_fill(struct GmdCtx *ctx, int nrow, int bb, int fltsiz, const int *lin,
+                  const int *col, const void *val, const long long *soff, int *Col, void *Val,
+                  int *err);
 int gmd_vec_diag(struct GmdCtx *ctx, const void *d, int ds, const void *u, void *v, int vs,
                  int b, int fltsiz, int nlin);
 
@@ -55,10 +53,6 @@ int gmd_vec_diag(struct GmdCtx *ctx, const void *d, int ds, const void *u, void 
 #endif
 
 #ifdef GML_INTERNAL_H
-int  gml_sell_build(int NmbLin, int BlkSiz, int FltSiz, const void *val, const int *col,
-                    const int *lin, GmlSell *s);
-void gml_sell_free(GmlSell *s);
-int  gml_sell_upload(GmlSct *gml, const GmlSell *s, GmlSellDev *d);
 void gml_sell_dev_free(GmlSct *gml, GmlSellDev *d);
 void gml_release_matrices(GmlSct *gml);
 void gml_release_solvers(GmlSct *gml);

@@ -273,3 +273,85 @@ extern "C" int gmd_vec_diag(GmdCtx *ctx, const void *d, int ds, const void *u, v
                                                      (double *)v, vs, b, nlin);
    return cudaGetLastError() == cudaSuccess;
 }
+
+/* ------------------------------------------------------------------------- */
+/* SELL-32 repack of a block CSR matrix on the device                         */
+/* ------------------------------------------------------------------------- */
+
+/* one warp per slice: row degrees and the slice width (longest row) */
+__global__ void __launch_bounds__(LA_THREADS)
+sell_width_kernel(int nrow, const int *__restrict__ lin, int *__restrict__ deg,
+                  long long *__restrict__ width, int *err)
+{
+   const int sl = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+   const int lane = threadIdx.x & 31, nsl = (nrow + 31) / 32;
+   if(sl >= nsl)
+      return;
+   const int r = sl * 32 + lane;
+   int d = 0;
+   if(r < nrow)
+   {
+      d = lin[r + 1] - lin[r];
+      if(d < 0)
+      {
+         atomicOr(err, 1);
+         d = 0;
+      }
+      deg[r] = d;
+   }
+   const int w = __reduce_max_sync(0xffffffffu, d);
+   if(lane == 0)
+      width[sl] = w;
+}
+
+/* one thread per row: entry k of row r goes to run (soff[slice] + k) of its
+   slice; out-of-range columns are reported and stored as column 0 with zero
+   values */
+template<class T>
+__global__ void __launch_bounds__(LA_THREADS)
+sell_fill_kernel(int nrow, int bb, const int *__restrict__ lin, const int *__restrict__ col,
+                 const T *__restrict__ val, const long long *__restrict__ soff,
+                 int *__restrict__ Col, T *__restrict__ Val, int *err)
+{
+   const int r = blockIdx.x * blockDim.x + threadIdx.x;
+   if(r >= nrow)
+      return;
+   const int lane = r & 31, b0 = lin[r], d = lin[r + 1] - b0;
+   const long long base = soff[r >> 5];
+   for(int k=0;k<d;k++)
+   {
+      const long long e = base + k;
+      const int c = col[b0 + k];
+      const bool ok = c >= 0 && c < nrow;
+      if(!ok)
+         atomicOr(err, 2);
+      Col[e * 32 + lane] = ok ? c : 0;
+      for(int v=0;v<bb;v++)
+         Val[(e * bb + v) * 32 + lane] = ok ? val[(size_t)(b0 + k) * bb + v] : (T)0;
+   }
+}
+
+extern "C" int gmd_sell_widths(GmdCtx *ctx, int nrow, const int *lin, int *deg, long long *width,
+                               int *err)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   const int nsl = (nrow + 31) / 32;
+   const unsigned g = (unsigned)(((long long)nsl * 32 + LA_THREADS - 1) / LA_THREADS);
+   sell_width_kernel<<<g, LA_THREADS, 0, st>>>(nrow, lin, deg, width, err);
+   return cudaGetLastError() == cudaSuccess;
+}
+
+extern "C" int gmd_sell_fill(GmdCtx *ctx, int nrow, int bb, int fltsiz, const int *lin,
+                             const int *col, const void *val, const long long *soff, int *Col,
+                             void *Val, int *err)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   const unsigned g = (unsigned)((nrow + LA_THREADS - 1) / LA_THREADS);
+   if(fltsiz == 4)
+      sell_fill_kernel<float><<<g, LA_THREADS, 0, st>>>(nrow, bb, lin, col, (const float *)val,
+                                                        soff, Col, (float *)Val, err);
+   else
+      sell_fill_kernel<double><<<g, LA_THREADS, 0, st>>>(nrow, bb, lin, col, (const double *)val,
+                                                         soff, Col, (double *)Val, err);
+   return cudaGetLastError() == cudaSuccess;
+}

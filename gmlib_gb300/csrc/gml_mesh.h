@@ -25,11 +25,13 @@ int gmd_mesh_point_count(struct GmdCtx *ctx, const void *tet, int nv, const int 
                          long long *width, long long *soff, int *err);
 int gmd_mesh_point_fill(struct GmdCtx *ctx, const void *tet, int nrow, const int *ptr,
                         const int *vt, const unsigned *rowv, const long long *soff, int *col);
+/* bps: resident blocks per SM for the persistent grid (0: the kernel's
+   maximum); a smaller grid leaves room for a concurrent kernel */
 int gmd_mesh_laplace(struct GmdCtx *ctx, int nrow, const unsigned *rowv, const long long *soff,
-                     const int *col, const void *in, void *out, float omega, int *err);
+                     const int *col, const void *in, void *out, float omega, int *err, int bps);
 int gmd_mesh_stats_init(struct GmdCtx *ctx, GmlxQualStats *st, int n);
 int gmd_mesh_quality(struct GmdCtx *ctx, int nt, const void *tet, const void *crd, float thr,
-                     float *qout, unsigned *flags, GmlxQualStats *st, int *err);
+                     float *qout, unsigned *flags, GmlxQualStats *st, int *err, int bps);
 
 /* batched meshes (gml_batch.c): a (mesh, range) tile queue drained by one
    persistent launch */

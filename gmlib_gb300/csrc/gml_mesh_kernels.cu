@@ -39,51 +39,6 @@
 #define MK_THREADS 256
 
 /* ========================================================================= */
-/* scans (single block, chunked; used for setup-sized arrays)                 */
-/* ========================================================================= */
-
-template<class T>
-__global__ void __launch_bounds__(1024) scan_excl_kernel(const T *in, T *out, int n)
-{
-   __shared__ T wsum[32];
-   __shared__ T carry;
-   int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-   if(tid == 0)
-      carry = 0;
-   __syncthreads();
-   for(int base=0;base<n;base+=1024)
-   {
-      int i = base + tid;
-      T x = i < n ? in[i] : (T)0, s = x;
-      for(int o=1;o<32;o<<=1)
-      {
-         T y = __shfl_up_sync(0xffffffffu, s, o);
-         if(lane >= o) s += y;
-      }
-      if(lane == 31) wsum[w] = s;
-      __syncthreads();
-      if(w == 0)
-      {
-         T ws = wsum[lane], t = ws;
-         for(int o=1;o<32;o<<=1)
-         {
-            T y = __shfl_up_sync(0xffffffffu, t, o);
-            if(lane >= o) t += y;
-         }
-         wsum[lane] = t - ws;
-      }
-      __syncthreads();
-      T excl = carry + wsum[w] + s - x;
-      if(i < n) out[i] = excl;
-      __syncthreads();
-      if(tid == 1023) carry = excl + x;
-      __syncthreads();
-   }
-   if(tid == 0)
-      out[n] = carry;
-}
-
-/* ========================================================================= */
 /* vertex -> tet CSR                                                          */
 /* ========================================================================= */
 
@@ -361,8 +316,12 @@ __device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes)
    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
 }
 
+#ifndef LP_BLOCKS
+#define LP_BLOCKS 6                        /* resident blocks per SM */
+#endif
+
 template<int U>
-__global__ void __launch_bounds__(MK_THREADS)
+__global__ void __launch_bounds__(MK_THREADS, LP_BLOCKS)
 laplace_pf_kernel(int nslice, const unsigned *__restrict__ rowv, const long long *__restrict__ soff,
                   const int *__restrict__ col, const float4 *__restrict__ in,
                   float4 *__restrict__ out, float omega)
@@ -682,10 +641,10 @@ __device__ __forceinline__ void qacc_add(QAcc &a, float q, int t, int f64)
 }
 
 #ifndef QK_HIST
-#define QK_HIST 0
+#define QK_HIST 1
 #endif
 #ifndef QK_L2ID
-#define QK_L2ID 0
+#define QK_L2ID 1
 #endif
 
 /* histogram update of a warp.  QK_HIST 0: lanes with the same bin add once
@@ -759,13 +718,13 @@ __device__ __forceinline__ void qacc_flush(QAcc &a, unsigned *hist, GmlxQualStat
 }
 
 #ifndef QK_CHUNK
-#define QK_CHUNK  512                      /* tets per stage: 8 KB */
+#define QK_CHUNK  1024                     /* tets per stage: 16 KB */
 #endif
 #ifndef QK_STAGES
-#define QK_STAGES 3
+#define QK_STAGES 2
 #endif
 #ifndef QK_BLOCKS
-#define QK_BLOCKS 6                        /* resident blocks per SM */
+#define QK_BLOCKS 5                        /* resident blocks per SM */
 #endif
 #define QK_SMEM   (QK_STAGES * QK_CHUNK * 16)
 
@@ -817,6 +776,7 @@ __device__ __forceinline__ void quality_pass(const int4 *chunk, int n, int start
       if(FULL || b1 < n) flags[ (start + b1) >> 5 ] = w1;
    }
 }
+
 
 template<bool WQ>
 __global__ void __launch_bounds__(MK_THREADS, QK_BLOCKS)
@@ -912,7 +872,8 @@ extern "C" int gmd_mesh_vt_csr(GmdCtx *ctx, const void *tet, int nt, int nv,
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
    cudaMemsetAsync(tmp, 0, (size_t)nv * sizeof(int), st);
    count_vt_kernel<<<nblk(nt, MK_THREADS), MK_THREADS, 0, st>>>((const int4 *)tet, nt, nv, tmp, err);
-   scan_excl_kernel<int><<<1, 1024, 0, st>>>(tmp, ptr, nv);
+   if(!gmd_scan_excl_i32(ctx, tmp, ptr, nv))
+      return 0;
    cudaMemsetAsync(tmp, 0, (size_t)nv * sizeof(int), st);
    fill_vt_kernel<<<nblk(nt, MK_THREADS), MK_THREADS, 0, st>>>((const int4 *)tet, nt, nv, ptr, tmp, vt);
    return cudaGetLastError() == cudaSuccess;
@@ -935,7 +896,8 @@ extern "C" int gmd_mesh_point_count(GmdCtx *ctx, const void *tet, int nv, const 
    point_count_kernel<<<nblk(nv, 128), 128, 0, st>>>(nv, (const int4 *)tet, ptr, vt, fixed, pdeg, err);
    window_sort_kernel<<<nwin, SIGMA, 0, st>>>(nv, pdeg, rowv);
    slice_width_kernel<<<nblk(nslice, MK_THREADS), MK_THREADS, 0, st>>>(nslice, rowv, width);
-   scan_excl_kernel<long long><<<1, 1024, 0, st>>>(width, soff, nslice);
+   if(!gmd_scan_excl_i64(ctx, width, soff, nslice))
+      return 0;
    return cudaGetLastError() == cudaSuccess;
 }
 
@@ -949,7 +911,8 @@ extern "C" int gmd_mesh_point_fill(GmdCtx *ctx, const void *tet, int nrow, const
 }
 
 extern "C" int gmd_mesh_laplace(GmdCtx *ctx, int nrow, const unsigned *rowv, const long long *soff,
-                                const int *col, const void *in, void *out, float omega, int *err)
+                                const int *col, const void *in, void *out, float omega, int *err,
+                                int bps)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
    static int attr_set = 0, variant = -1;
@@ -963,7 +926,8 @@ extern "C" int gmd_mesh_laplace(GmdCtx *ctx, int nrow, const unsigned *rowv, con
    if(variant >= 2)
    {
       const int nslice = nrow / 32;
-      long long need = nblk(nslice, MK_THREADS / 32), cap2 = (long long)gmd_num_sms(ctx) * 6;
+      long long need = nblk(nslice, MK_THREADS / 32);
+      long long cap2 = (long long)gmd_num_sms(ctx) * (bps > 0 && bps < LP_BLOCKS ? bps : LP_BLOCKS);
       unsigned g2 = (unsigned)(need < cap2 ? need : cap2);
       if(variant == 2)
          laplace_pf_kernel<4><<<g2, MK_THREADS, 0, st>>>(nslice, rowv, soff, col, (const float4 *)in,
@@ -1003,12 +967,12 @@ extern "C" int gmd_mesh_stats_init(GmdCtx *ctx, GmlxQualStats *st, int n)
 }
 
 extern "C" int gmd_mesh_quality(GmdCtx *ctx, int nt, const void *tet, const void *crd, float thr,
-                                float *qout, unsigned *flags, GmlxQualStats *st, int *err)
+                                float *qout, unsigned *flags, GmlxQualStats *st, int *err, int bps)
 {
    static int attr_set = 0;
    cudaStream_t s = (cudaStream_t)gmd_stream(ctx);
    long long need = nblk(nt, QK_CHUNK);
-   long long cap = (long long)gmd_num_sms(ctx) * QK_BLOCKS;
+   long long cap = (long long)gmd_num_sms(ctx) * (bps > 0 && bps < QK_BLOCKS ? bps : QK_BLOCKS);
    unsigned g = (unsigned)(need < cap ? need : cap);
    if(nt <= 0)
       return 1;

@@ -13,6 +13,16 @@
 
 #include "gml_native.h"
 
+/* measured on the 128^3 smoothing step: the quality pass on 2 blocks per
+   SM beside the sweep on 3 overlaps best (1.31 ms against 1.42 ms with
+   both on their full grids) */
+#ifndef GML_SPLIT_Q
+#define GML_SPLIT_Q 2
+#endif
+#ifndef GML_SPLIT_L
+#define GML_SPLIT_L 3
+#endif
+
 NatSct *gmlx_nat(GmlSct *gml)
 {
    if(!gml->ext)
@@ -213,7 +223,7 @@ static int sweeps(GmlSct *gml, NatSct *n, GmlDatSct *ver, int ns, float omega)
    void *a = ver->GpuMem, *b = n->crd2;
    for(int s=0;s<ns;s++)
    {
-      if(!gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, a, b, omega, n->err))
+      if(!gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, a, b, omega, n->err, 0))
          return 0;
       void *t = a; a = b; b = t;
    }
@@ -291,7 +301,7 @@ int GmlxQualityStats(size_t GmlIdx, double h, int QalIdx, GmlxQuality *res)
    gml_lib_timer_begin(gml, &gml->krn[ n->NmbQalKrn ]);
    gmd_mesh_stats_init(gml->dev, n->stats, 1);
    if(!gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, ver->GpuMem, gmlx_det_threshold(h),
-                        q ? (float *)q->GpuMem : NULL, n->flags, n->stats, n->err))
+                        q ? (float *)q->GpuMem : NULL, n->flags, n->stats, n->err, 0))
       return 0;
    gml_lib_timer_end(gml, &gml->krn[ n->NmbQalKrn ]);
    if(res)
@@ -316,12 +326,25 @@ int GmlxInvertedFlags(size_t GmlIdx, unsigned *flags, size_t nwords)
    return gmd_d2h(gml->dev, flags, n->flags, need * sizeof(unsigned));
 }
 
+/* resident blocks per SM of the quality pass and of the sweep when they run
+   side by side in the graph (0: each kernel's maximum; GML_SPLIT="q,l"
+   overrides, for tuning) */
+static void graph_split(int *qb, int *lb)
+{
+   const char *e = getenv("GML_SPLIT");
+   *qb = GML_SPLIT_Q;
+   *lb = GML_SPLIT_L;
+   if(e && sscanf(e, "%d,%d", qb, lb) != 2)
+      *qb = *lb = 0;
+}
+
 int GmlxSmoothQualityLoop(size_t GmlIdx, int nsweeps, float omega, double h, GmlxQuality *res)
 {
    GETGMLPTR(gml, GmlIdx);
    NatSct *n;
    GmlDatSct *ver, *tet;
    GmlxQualStats *st;
+   int qb = 0, lb = 0;
 
    if(!ready(gml, &n, &ver, &tet) || nsweeps < 1 || nsweeps > n->nstats)
       return 0;
@@ -342,11 +365,12 @@ int GmlxSmoothQualityLoop(size_t GmlIdx, int nsweeps, float omega, double h, Gml
             n->evL[e] = gmd_event_new_sync();
             n->evQ[e] = gmd_event_new_sync();
          }
+      graph_split(&qb, &lb);
       if(!gmd_graph_begin(gml->dev))
          return 0;
       gmd_mesh_stats_init(gml->dev, n->stats, nsweeps);
       gmd_event_record(gml->dev, n->evL[0]);
-      gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, a, b, omega, n->err);
+      gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, a, b, omega, n->err, 0);
       gmd_event_record(gml->dev, n->evL[1]);
       for(int s=1;s<=nsweeps;s++)
       {
@@ -354,14 +378,14 @@ int GmlxSmoothQualityLoop(size_t GmlIdx, int nsweeps, float omega, double h, Gml
          gmd_use_side(gml->dev, 1);
          gmd_stream_wait(gml->dev, n->evL[s]);
          gmd_mesh_quality(gml->dev, n->nt, tet->GpuMem, xs, gmlx_det_threshold(h), NULL, n->flags,
-                          n->stats + s - 1, n->err);
+                          n->stats + s - 1, n->err, qb);
          gmd_event_record(gml->dev, n->evQ[s]);
          gmd_use_side(gml->dev, 0);
          if(s < nsweeps)
          {
             if(s >= 2)
                gmd_stream_wait(gml->dev, n->evQ[s-1]);
-            gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, xs, xn, omega, n->err);
+            gmd_mesh_laplace(gml->dev, n->nrow, n->rowv, n->soff, n->pcol, xs, xn, omega, n->err, lb);
             gmd_event_record(gml->dev, n->evL[s+1]);
          }
       }

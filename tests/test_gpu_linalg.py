@@ -164,3 +164,24 @@ def test_cg_breakdown_and_errors(gpu):
     ix = new_vector(gpu, np.zeros_like(rhs), G.GmlDbl)
     assert G.lib.GmlxSolveCG(gpu, m32, ib, ix, 0, 1e-10, 10, None) == -3
     assert G.lib.GmlxSolveCG(gpu, 9, ib, ix, 0, 1e-10, 10, None) == -1
+
+
+@pytest.mark.gpu
+def test_new_matrix_rejects_bad_csr(gpu):
+    """Column indices outside the rows and decreasing row pointers are
+    caught by the device repack: GmlNewMatrix returns 0 and the slot is
+    free for the next matrix."""
+    rng = np.random.default_rng(4)
+    lin, col, val = random_bsr(rng, 200, 3, maxdeg=6)
+    bad = col.copy()
+    bad[len(bad) // 2] = 200
+    IP = ctypes.POINTER(ctypes.c_int)
+    v = np.ascontiguousarray(val)
+    assert G.lib.GmlNewMatrix(gpu, 200, len(col), 3, G.as_ptr(v), bad.ctypes.data_as(IP),
+                              lin.ctypes.data_as(IP), G.GmlDbl) == 0
+    lin2 = lin.copy()
+    lin2[100], lin2[101] = lin2[101], lin2[100]
+    if lin2[100] != lin2[101]:
+        assert G.lib.GmlNewMatrix(gpu, 200, len(col), 3, G.as_ptr(v), col.ctypes.data_as(IP),
+                                  lin2.ctypes.data_as(IP), G.GmlDbl) == 0
+    assert new_matrix(gpu, lin, col, val, G.GmlDbl) == 1
