@@ -615,6 +615,31 @@ def run_serve(args, dist):
         ser[i].kind, ser[i].target, ser[i].arrival = req[i].kind, req[i].target, req[i].arrival
     sts = G.GmlxServeStats()
     G.lib.GmlxServeRun(srv, ser, nser, G.GmlxServeSerial, ctypes.byref(sts))
+    def breakdown(reqs, n):
+        """per kind: mean queueing delay (start - arrival) and service time
+        (finish - start), split by whether the request loaded its target"""
+        out = {}
+        firsts = set()
+        loaded = []
+        for i in range(n):
+            t = reqs[i].target
+            loaded.append(t not in firsts)
+            firsts.add(t)
+        names = {G.GmlxReqQuality: "quality", G.GmlxReqSmooth: "smooth", G.GmlxReqSolve: "solve"}
+        for k, name in names.items():
+            for cold in (True, False):
+                idx = [i for i in range(n) if reqs[i].kind == k and loaded[i] == cold
+                       and reqs[i].status == 1]
+                if not idx:
+                    continue
+                q = [reqs[i].start - reqs[i].arrival for i in idx]
+                sv = sorted(reqs[i].finish - reqs[i].start for i in idx)
+                out["%s_%s" % (name, "load" if cold else "resident")] = {
+                    "n": len(idx), "queue_ms": round(1e3 * sum(q) / len(q), 2),
+                    "service_ms": round(1e3 * sum(sv) / len(sv), 2),
+                    "service_p99_ms": round(1e3 * sv[int(0.99 * (len(sv) - 1))], 2)}
+        return out
+    bd = breakdown(req, nreq)
     same = sum(1 for i in range(nser)
                if req[i].status == 1 and ser[i].status == 1
                and (req[i].NmbIte, req[i].RelRes, req[i].qal.MinQal, req[i].qal.MinIdx)
@@ -635,7 +660,7 @@ def run_serve(args, dist):
                                        "10-sweep smoothing / CG (1e-10)" % (args.rate, args.duration),
                            "sizes_tets": [int(6 * n ** 3) for n in ns], "reuse": 0.5,
                            "budget_gb": 150, "slots": 8, "pool_generation_s": round(tgen, 1)},
-                "batching": d(stb), "serial_prefix": d(sts),
+                "batching": d(stb), "batching_by_kind": bd, "serial_prefix": d(sts),
                 "same_result_alone_and_in_mix": "%d of %d" % (same, nser), "clocks": clk}
         print(json.dumps(line), flush=True)
 

@@ -307,7 +307,7 @@ int GmlxSetData(size_t GmlIdx, int DatIdx, const void *buf, size_t bytes)
    if(!dat || !dat->CpuMem || bytes != dat->MemSiz)
       return 0;
    gml_wait_upload(gml, dat);
-   memcpy(dat->CpuMem, buf, bytes);
+   gml_host_copy(dat->CpuMem, buf, bytes);
    return gml_upload(gml, DatIdx) || !bytes;
 }
 
@@ -319,7 +319,7 @@ int GmlxGetData(size_t GmlIdx, int DatIdx, void *buf, size_t bytes)
       return 0;
    if(!gml_download(gml, DatIdx) && bytes)
       return 0;
-   memcpy(buf, dat->CpuMem, bytes);
+   gml_host_copy(buf, dat->CpuMem, bytes);
    return 1;
 }
 

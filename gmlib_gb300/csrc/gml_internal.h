@@ -150,6 +150,7 @@ int   gml_upload(GmlSct *gml, int idx);
 int   gml_download(GmlSct *gml, int idx);
 void  gml_wait_upload(GmlSct *gml, GmlDatSct *dat);
 int   gml_new_kernel_slot(GmlSct *gml, int kind, const char *name);
+void  gml_host_copy(void *dst, const void *src, size_t n);     /* gml_hostcopy.c */
 int   gml_timed_launch(GmlSct *gml, GmlKrnSct *krn, unsigned grid, unsigned block, void **args);
 void  gml_lib_timer_begin(GmlSct *gml, GmlKrnSct *krn);
 void  gml_lib_timer_end(GmlSct *gml, GmlKrnSct *krn);

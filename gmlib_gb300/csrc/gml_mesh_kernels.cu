@@ -319,6 +319,9 @@ __device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes)
 #ifndef LP_BLOCKS
 #define LP_BLOCKS 6                        /* resident blocks per SM */
 #endif
+#ifndef LP_PFDIST
+#define LP_PFDIST 1                        /* L2 prefetch distance, in slices per warp */
+#endif
 
 template<int U>
 __global__ void __launch_bounds__(MK_THREADS, LP_BLOCKS)
@@ -330,16 +333,23 @@ laplace_pf_kernel(int nslice, const unsigned *__restrict__ rowv, const long long
    const int w0 = (blockIdx.x * MK_THREADS + threadIdx.x) >> 5;
    const int nw = (gridDim.x * MK_THREADS) >> 5;
 
-   if(lane == 0 && w0 < nslice)
-   {
-      const long long c0 = __ldg(&soff[w0]), c1 = __ldg(&soff[w0 + 1]);
-      if(c1 > c0)
-         prefetch_l2(col + c0 * 32, (unsigned)((c1 - c0) * 128));
-   }
+   /* the column runs of the first LP_PFDIST slices, then one slice
+      LP_PFDIST iterations ahead of the current one */
+   if(lane == 0)
+      for(int k=0;k<LP_PFDIST;k++)
+      {
+         const int s0 = w0 + k * nw;
+         if(s0 < nslice)
+         {
+            const long long c0 = __ldg(&soff[s0]), c1 = __ldg(&soff[s0 + 1]);
+            if(c1 > c0)
+               prefetch_l2(col + c0 * 32, (unsigned)((c1 - c0) * 128));
+         }
+      }
 
    for(int sl=w0; sl<nslice; sl+=nw)
    {
-      const int nx = sl + nw;
+      const int nx = sl + LP_PFDIST * nw;
       if(lane == 0 && nx < nslice)
       {
          const long long c0 = __ldg(&soff[nx]), c1 = __ldg(&soff[nx + 1]);
@@ -609,12 +619,14 @@ __device__ __forceinline__ float tet_mean_ratio(const int4 e, const float4 *__re
       the absolute values of its six products, a sum bounded by
       (|ab|_1 |ac|_1 |ad|_1) <= l2^(3/2); below 16 eps32 l2^(3/2) (1% margin
       for rsqrt) the sign is taken from the FP64 determinant. */
-   *f64 = 0;
-   if(fabsf(det) < fmaxf(thr, 9.7e-07f * l2 * l2 * rsqrtf_fast(l2)))
-   {
+   const bool need = fabsf(det) < fmaxf(thr, 9.7e-07f * l2 * l2 * rsqrtf_fast(l2));
+   *f64 = need;
+#if QK_UNIFORM
+   /* the rare FP64 path behind a warp-uniform test */
+   if(__any_sync(__activemask(), need))
+#endif
+   if(need)
       pos = det64_positive(a, b, c, d, &det);
-      *f64 = 1;
-   }
    const float v23 = exp2f_fast(0.6666666865f * log2f_fast(0.5f * fabsf(det)));
    const float q = __fdividef(12.0f * v23, l2);
    *inv = !pos;
@@ -645,6 +657,9 @@ __device__ __forceinline__ void qacc_add(QAcc &a, float q, int t, int f64)
 #endif
 #ifndef QK_L2ID
 #define QK_L2ID 1
+#endif
+#ifndef QK_UNIFORM
+#define QK_UNIFORM 0
 #endif
 
 /* histogram update of a warp.  QK_HIST 0: lanes with the same bin add once
@@ -724,7 +739,7 @@ __device__ __forceinline__ void qacc_flush(QAcc &a, unsigned *hist, GmlxQualStat
 #define QK_STAGES 2
 #endif
 #ifndef QK_BLOCKS
-#define QK_BLOCKS 5                        /* resident blocks per SM */
+#define QK_BLOCKS 4                        /* resident blocks per SM */
 #endif
 #define QK_SMEM   (QK_STAGES * QK_CHUNK * 16)
 
@@ -921,7 +936,8 @@ extern "C" int gmd_mesh_laplace(GmdCtx *ctx, int nrow, const unsigned *rowv, con
    {
       /* GML_LAPLACE = sell, tma, pf or pf8 selects the sweep kernel (default pf8) */
       const char *e = getenv("GML_LAPLACE");
-      variant = !e ? 3 : !strcmp(e, "sell") ? 1 : !strcmp(e, "tma") ? 0 : !strcmp(e, "pf") ? 2 : 3;
+      variant = !e ? 3 : !strcmp(e, "sell") ? 1 : !strcmp(e, "tma") ? 0 : !strcmp(e, "pf") ? 2
+              : !strcmp(e, "pf16") ? 4 : 3;
    }
    if(variant >= 2)
    {
@@ -932,6 +948,9 @@ extern "C" int gmd_mesh_laplace(GmdCtx *ctx, int nrow, const unsigned *rowv, con
       if(variant == 2)
          laplace_pf_kernel<4><<<g2, MK_THREADS, 0, st>>>(nslice, rowv, soff, col, (const float4 *)in,
                                                          (float4 *)out, omega);
+      else if(variant == 4)
+         laplace_pf_kernel<16><<<g2, MK_THREADS, 0, st>>>(nslice, rowv, soff, col, (const float4 *)in,
+                                                          (float4 *)out, omega);
       else
          laplace_pf_kernel<8><<<g2, MK_THREADS, 0, st>>>(nslice, rowv, soff, col, (const float4 *)in,
                                                          (float4 *)out, omega);
@@ -1022,8 +1041,22 @@ __device__ __forceinline__ void batch_sweep_slices(int s0, int s1, const unsigne
                                                    const float4 *in, float4 *out, float omega)
 {
    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+   if(lane == 0 && s0 + wid < s1)
+   {
+      const long long c0 = __ldg(&soff[s0 + wid]), c1 = __ldg(&soff[s0 + wid + 1]);
+      if(c1 > c0)
+         prefetch_l2(col + c0 * 32, (unsigned)((c1 - c0) * 128));
+   }
    for(int sl=s0+wid; sl<s1; sl+=MK_THREADS/32)
    {
+      /* the next slice of this warp: its column run into L2 */
+      const int nx = sl + MK_THREADS / 32;
+      if(lane == 0 && nx < s1)
+      {
+         const long long c0 = __ldg(&soff[nx]), c1 = __ldg(&soff[nx + 1]);
+         if(c1 > c0)
+            prefetch_l2(col + c0 * 32, (unsigned)((c1 - c0) * 128));
+      }
       const unsigned pk = __ldg(&rowv[ sl * 32 + lane ]);
       if(pk == ROW_NONE)
          continue;

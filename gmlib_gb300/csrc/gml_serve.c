@@ -166,11 +166,8 @@ static int load(SrvSct *s, SrvTarget *t)
    if(!g)
       return 0;
    GmlxSetTiming(g, 0);
-   /* short-lived instances: no messages, and pageable host mirrors (page
-      locking and unlocking them would cost more than the uploads they speed
-      up, and freeing pinned memory synchronises the whole device) */
+   /* no informational messages from served instances */
    ((GmlSct *)g)->Quiet = 1;
-   ((GmlSct *)g)->PinOff = 1;
    t->g = g;
    if(t->kind == 0)
    {
