@@ -503,7 +503,7 @@ def run_batch(args, dist):
         raise SystemExit("GmlxBatchSetup failed")
     sweeps, om = 5, ctypes.c_float(OMEGA)
     G.lib.GmlxBatchTune(g, sweeps, om)
-    ts_, tt_, gr_, ntile = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    ts_, tt_, gr_, ntile, wt_ = (ctypes.c_int() for _ in range(5))
     res = (G.GmlxQuality * len(ms))()
     e0, e1 = G.lib.GmlxEventCreate(), G.lib.GmlxEventCreate()
     out = {}
@@ -523,7 +523,7 @@ def run_batch(args, dist):
     clk = clocks.stop()
     G.lib.GmlxBatchRun(g, sweeps, om, G.GmlxBatchQueue, res)
     G.lib.GmlxBatchInfo(g, ctypes.byref(ts_), ctypes.byref(tt_), ctypes.byref(gr_),
-                        ctypes.byref(ntile))
+                        ctypes.byref(ntile), ctypes.byref(wt_))
     stored, used, mx = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
     G.lib.GmlxMeshBallInfo(g, ctypes.byref(stored), ctypes.byref(used), ctypes.byref(mx))
     vpad = float(sum((int(v) + 255) // 256 * 256 for v in nv))
@@ -543,7 +543,8 @@ def run_batch(args, dist):
                            "generation_s": round(tgen, 1)},
                 "queue": out["queue"], "loop": out["loop"],
                 "speedup_vs_loop": round(out["loop"]["ms_per_run"] / out["queue"]["ms_per_run"], 2),
-                "tiles": {"slices_per_sweep_tile": ts_.value, "tets_per_quality_tile": tt_.value,
+                "tiles": {"claimed_per": "warp" if wt_.value else "block",
+                          "slices_per_sweep_tile": ts_.value, "tets_per_quality_tile": tt_.value,
                           "grid": gr_.value, "tiles": ntile.value},
                 "roofline": {"bound": "hbm", "algorithmic_bytes_per_run": byts,
                              "achieved": round(byts / tq / 1e9, 1), "peak": peak,

@@ -163,7 +163,8 @@ SIGNATURES.update({
     "GmlxBatchGetMesh": (_i, [_s, _i, _p]),
     "GmlxBatchFlags": (_i, [_s, _i, _p, _s]),
     "GmlxBatchTune": (_i, [_s, _i, _f]),
-    "GmlxBatchInfo": (_i, [_s, _ip, _ip, _ip, _ip]),
+    "GmlxBatchSetTiles": (_i, [_s, _i, _i, _i, _i]),
+    "GmlxBatchInfo": (_i, [_s, _ip, _ip, _ip, _ip, _ip]),
     "GmlxServeNew": (_s, [_i, _d, _i]),
     "GmlxServeAddMesh": (_i, [_s, _i, _p, _p, _i, _p, _d]),
     "GmlxServeAddSystem": (_i, [_s, _i, _i, _p, _p, _p, _p]),

@@ -24,9 +24,9 @@
  * arithmetic per vertex and the quality per tet are the same; only the FP64
  * sum of the qualities depends on the accumulation order.
  *
- * Tuning.  GmlxBatchTune times the queue with a few tile sizes and grid
- * sizes on the packed meshes (restoring the coordinates afterwards) and
- * keeps the fastest.
+ * Tuning.  GmlxBatchTune times the queue on the packed meshes (restoring
+ * the coordinates afterwards) with tiles claimed per block or per warp,
+ * several tile sizes and two grid sizes, and keeps the fastest.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -46,6 +46,7 @@ typedef struct
    int            *need, *done, *ctl;      /* ctl: head, abort, err */
    int            ntile, nphase, tsweeps;
    int            tile_slices, tile_tets, grid, maxgrid;
+   int            warp;                   /* 1: tiles claimed per warp */
    unsigned       *flags;
    GmlxQualStats  *stats, *hstats;
    void           *graph;
@@ -367,7 +368,8 @@ static int bat_queue_work(GmlSct *gml, BatSct *b, NatSct *n, int nsweeps, float 
    return gmd_memset_async(gml->dev, b->ctl, 0, 2 * sizeof(int))
        && gmd_memset_async(gml->dev, b->done, 0, (size_t)b->nmesh * b->nphase * sizeof(int))
        && gmd_mesh_stats_init(gml->dev, b->stats, b->nmesh)
-       && gmd_batch_queue(gml->dev, &a, b->grid)
+       && (b->warp ? gmd_batch_queue_warp(gml->dev, &a, b->grid)
+                   : gmd_batch_queue(gml->dev, &a, b->grid))
        && (!(nsweeps & 1) || gmd_d2d_async(gml->dev, vd->GpuMem, n->crd2, (size_t)b->nv * 16));
 }
 
@@ -480,13 +482,18 @@ int GmlxBatchFlags(size_t GmlIdx, int MshIdx, unsigned *flags, size_t nwords)
 int GmlxBatchTune(size_t GmlIdx, int nsweeps, float omega)
 {
    GETGMLPTR(gml, GmlIdx);
-   static const int cand[][2] = { { 8, 2048 }, { 32, 4096 }, { 128, 16384 } };
+   /* (tiles per warp or per block, slices per sweep tile, tets per quality
+      tile, grid as a fraction of the resident maximum: 2 full, 1 half) */
+   static const int cand[][4] = {
+      { 0, 8, 2048, 2 }, { 0, 32, 4096, 2 }, { 0, 128, 16384, 2 }, { 0, 32, 4096, 1 },
+      { 1, 2, 512, 2 },  { 1, 4, 1024, 2 },  { 1, 16, 4096, 2 },   { 1, 4, 1024, 1 } };
+   const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
    BatSct *b;
    NatSct *n;
    GmlDatSct *vd;
    void *save, *e0, *e1;
    double best = 1e30;
-   int bs = 0, bt = 0, bg = 0, c, gsel;
+   int bs = 0, bt = 0, bg = 0, bw = 0, c;
 
    if(!bat_ready(gml, &b, &n) || nsweeps < 0)
       return 0;
@@ -502,30 +509,31 @@ int GmlxBatchTune(size_t GmlIdx, int nsweeps, float omega)
       return 0;
    }
    gmd_d2d_async(gml->dev, save, vd->GpuMem, (size_t)b->nv * 16);
-   bs = b->tile_slices; bt = b->tile_tets; bg = b->grid;
-   for(c=0;c<3;c++)
-      for(gsel=0;gsel<2;gsel++)
+   bs = b->tile_slices; bt = b->tile_tets; bg = b->grid; bw = b->warp;
+   for(c=0;c<ncand;c++)
+   {
+      double t;
+      b->warp = cand[c][0];
+      b->tile_slices = cand[c][1];
+      b->tile_tets = cand[c][2];
+      b->grid = cand[c][3] == 2 ? b->maxgrid : (b->maxgrid + 1) / 2;
+      bat_free_tiles(gml, b);
+      if(!GmlxBatchRun(GmlIdx, nsweeps, omega, GmlxBatchQueue, NULL))
+         continue;
+      gmd_event_record(gml->dev, e0);
+      GmlxBatchRun(GmlIdx, nsweeps, omega, GmlxBatchQueue, NULL);
+      gmd_event_record(gml->dev, e1);
+      t = gmd_event_elapsed_s(e0, e1);
+      if(t < best)
       {
-         double t;
-         b->tile_slices = cand[c][0];
-         b->tile_tets = cand[c][1];
-         b->grid = gsel ? (b->maxgrid + 1) / 2 : b->maxgrid;
-         bat_free_tiles(gml, b);
-         if(!GmlxBatchRun(GmlIdx, nsweeps, omega, GmlxBatchQueue, NULL))
-            continue;
-         gmd_event_record(gml->dev, e0);
-         GmlxBatchRun(GmlIdx, nsweeps, omega, GmlxBatchQueue, NULL);
-         gmd_event_record(gml->dev, e1);
-         t = gmd_event_elapsed_s(e0, e1);
-         if(t < best)
-         {
-            best = t;
-            bs = b->tile_slices; bt = b->tile_tets; bg = b->grid;
-         }
+         best = t;
+         bs = b->tile_slices; bt = b->tile_tets; bg = b->grid; bw = b->warp;
       }
+   }
    b->tile_slices = bs;
    b->tile_tets = bt;
    b->grid = bg;
+   b->warp = bw;
    bat_free_tiles(gml, b);
    gmd_d2d_async(gml->dev, vd->GpuMem, save, (size_t)b->nv * 16);
    gmd_sync(gml->dev);
@@ -535,7 +543,23 @@ int GmlxBatchTune(size_t GmlIdx, int nsweeps, float omega)
    return 1;
 }
 
-int GmlxBatchInfo(size_t GmlIdx, int *TileSlices, int *TileTets, int *grid, int *ntile)
+int GmlxBatchSetTiles(size_t GmlIdx, int WarpTiles, int TileSlices, int TileTets, int grid)
+{
+   GETGMLPTR(gml, GmlIdx);
+   BatSct *b = bat(gml);
+   if(!b || TileSlices < 1 || TileTets < 32 || (TileTets & 31) || grid < 0)
+      return 0;
+   b->warp = WarpTiles ? 1 : 0;
+   b->tile_slices = TileSlices;
+   b->tile_tets = TileTets;
+   if(grid > 0)
+      b->grid = grid;
+   bat_free_tiles(gml, b);
+   return 1;
+}
+
+int GmlxBatchInfo(size_t GmlIdx, int *TileSlices, int *TileTets, int *grid, int *ntile,
+                  int *WarpTiles)
 {
    GETGMLPTR(gml, GmlIdx);
    BatSct *b = bat(gml);
@@ -545,5 +569,6 @@ int GmlxBatchInfo(size_t GmlIdx, int *TileSlices, int *TileTets, int *grid, int 
    if(TileTets) *TileTets = b->tile_tets;
    if(grid) *grid = b->grid;
    if(ntile) *ntile = b->ntile;
+   if(WarpTiles) *WarpTiles = b->warp;
    return 1;
 }

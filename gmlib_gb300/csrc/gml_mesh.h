@@ -55,7 +55,8 @@ typedef struct
    float                omega;
 }GmdBatchArgs;
 
-int gmd_batch_queue(struct GmdCtx *ctx, const GmdBatchArgs *a, int grid);
+int gmd_batch_queue(struct GmdCtx *ctx, const GmdBatchArgs *a, int grid);       /* block tiles */
+int gmd_batch_queue_warp(struct GmdCtx *ctx, const GmdBatchArgs *a, int grid);  /* warp tiles */
 int gmd_batch_grid(struct GmdCtx *ctx);
 int gmd_mesh_laplace_slices(struct GmdCtx *ctx, int s0, int s1, const unsigned *rowv,
                             const long long *soff, const int *col, const void *in, void *out,

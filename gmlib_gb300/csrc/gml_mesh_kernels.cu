@@ -1206,6 +1206,222 @@ batch_queue_kernel(GmdBatchArgs a)
    }
 }
 
+/* The same queue drained by warps instead of blocks: each warp claims its
+   own tiles, waits for its own dependencies and counts its tiles done, so
+   no block barrier sits in the tile loop.  Quality statistics are folded
+   per warp (registers and a per-warp histogram) and flushed per tile. */
+__device__ __forceinline__ void warp_sweep_slices(int s0, int s1, const unsigned *__restrict__ rowv,
+                                                  const long long *__restrict__ soff,
+                                                  const int *__restrict__ col,
+                                                  const float4 *in, float4 *out, float omega)
+{
+   const int lane = threadIdx.x & 31;
+   if(lane == 0)
+   {
+      const long long c0 = __ldg(&soff[s0]), c1 = __ldg(&soff[s0 + 1]);
+      if(c1 > c0)
+         prefetch_l2(col + c0 * 32, (unsigned)((c1 - c0) * 128));
+   }
+   for(int sl=s0; sl<s1; sl++)
+   {
+      if(lane == 0 && sl + 1 < s1)
+      {
+         const long long c0 = __ldg(&soff[sl + 1]), c1 = __ldg(&soff[sl + 2]);
+         if(c1 > c0)
+            prefetch_l2(col + c0 * 32, (unsigned)((c1 - c0) * 128));
+      }
+      const unsigned pk = __ldg(&rowv[ sl * 32 + lane ]);
+      if(pk == ROW_NONE)
+         continue;
+      const int v = (int)(pk & ROW_MASK), d = (int)(pk >> ROW_SHIFT);
+      const float4 p = __ldcg(&in[v]);
+      if(d == 0)
+      {
+         out[v] = p;
+         continue;
+      }
+      const int *cp = col + __ldg(&soff[sl]) * 32 + lane;
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      int c[8];
+#pragma unroll
+      for(int u=0;u<8;u++)
+         c[u] = u < d ? __ldg(cp + u * 32) : 0;
+      for(int k=0;k<d;k+=8)
+      {
+         int nc[8];
+#pragma unroll
+         for(int u=0;u<8;u++)
+            nc[u] = k + 8 + u < d ? __ldg(cp + (size_t)(k + 8 + u) * 32) : 0;
+#pragma unroll
+         for(int u=0;u<8;u++)
+            if(k + u < d)
+            {
+               const float4 q = __ldcg(&in[ c[u] ]);
+               sx += q.x; sy += q.y; sz += q.z;
+            }
+#pragma unroll
+         for(int u=0;u<8;u++)
+            c[u] = nc[u];
+      }
+      const float inv = 1.0f / (float)d;
+      out[v] = make_float4(p.x + omega * (sx * inv - p.x), p.y + omega * (sy * inv - p.y),
+                           p.z + omega * (sz * inv - p.z), 0.f);
+   }
+}
+
+__device__ __forceinline__ void warp_quality_range(int beg, int end, const int4 *__restrict__ tet,
+                                                   const float4 *crd, float thr,
+                                                   unsigned *__restrict__ flags, QAcc &a,
+                                                   unsigned *hist)
+{
+   const int lane = threadIdx.x & 31;
+   for(int base=beg; base<end; base+=32)
+   {
+      const int j = base + lane;
+      const bool v = j < end;
+      int inv = 0, f = 0;
+      float q = 0.f;
+      if(v)
+      {
+         q = tet_mean_ratio<true>(__ldg(&tet[j]), crd, thr, &inv, &f);
+         if(q < a.mn) { a.mn = q; a.mi = j; }
+         if(q > a.mx) { a.mx = q; a.xi = j; }
+         const float tt = a.s + q, bp = tt - a.s;
+         a.c += (a.s - (tt - bp)) + (q - bp);
+         a.s = tt;
+         a.nf64 += f;
+         int bin = (int)(q * 64.0f);
+         bin = bin < 0 ? 0 : (bin > 63 ? 63 : bin);
+         atomicAdd(&hist[bin], 1u);
+      }
+      const unsigned w = __ballot_sync(0xffffffffu, inv);
+      if(lane == 0)
+      {
+         a.ninv += __popc(w);
+         flags[ base >> 5 ] = w;
+      }
+   }
+}
+
+/* warp reduction of the accumulators into a mesh's statistics; resets them */
+__device__ __forceinline__ void warp_flush(QAcc &a, unsigned *hist, GmlxQualStats *st)
+{
+   const int lane = threadIdx.x & 31;
+   double dsum = (double)a.s + (double)a.c;
+   unsigned long long kmin = ~0ULL, kmax = ~0ULL;
+   unsigned ninv = a.ninv, nf64 = a.nf64;
+   if(a.mi >= 0)
+   {
+      const unsigned k = mk_fkey(a.mn), kx = mk_fkey(a.mx);
+      kmin = ((unsigned long long)k << 32) | (unsigned)a.mi;
+      kmax = ((unsigned long long)(~kx) << 32) | (unsigned)a.xi;
+   }
+   for(int o=16;o>0;o>>=1)
+   {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, kmin, o);
+      const unsigned long long y = __shfl_xor_sync(0xffffffffu, kmax, o);
+      kmin = x < kmin ? x : kmin;
+      kmax = y < kmax ? y : kmax;
+      dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+      nf64 += __shfl_xor_sync(0xffffffffu, nf64, o);
+      ninv += __shfl_xor_sync(0xffffffffu, ninv, o);
+   }
+   if(lane == 0)
+   {
+      atomicMin(&st->MinKey, kmin);
+      atomicMin(&st->MaxKey, kmax);
+      atomicAdd(&st->Sum, dsum);
+      atomicAdd(&st->NmbInv, ninv);
+      atomicAdd(&st->NmbF64, nf64);
+   }
+   __syncwarp();
+   for(int b=lane;b<64;b+=32)
+   {
+      if(hist[b])
+         atomicAdd(&st->Hist[b], hist[b]);
+      hist[b] = 0;
+   }
+   __syncwarp();
+   a = QAcc{ 3.402823466e38f, -3.402823466e38f, 0.f, 0.f, -1, -1, 0u, 0u };
+}
+
+__global__ void __launch_bounds__(MK_THREADS)
+batch_warp_kernel(GmdBatchArgs a)
+{
+   __shared__ unsigned hist_all[MK_THREADS / 32][64];
+   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+   unsigned *hist = hist_all[wid];
+   QAcc acc = { 3.402823466e38f, -3.402823466e38f, 0.f, 0.f, -1, -1, 0u, 0u };
+   float4 *b0 = (float4 *)a.buf0, *b1 = (float4 *)a.buf1;
+
+   for(int b=lane;b<64;b+=32)
+      hist[b] = 0;
+   __syncwarp();
+   for(;;)
+   {
+      int t = -1;
+      if(lane == 0)
+      {
+         if(!*(volatile int *)a.abort)
+            t = atomicAdd(a.head, 1);
+         if(t >= a.ntile)
+            t = -1;
+         if(t >= 0)
+         {
+            const GmdBatchTile tl = a.tiles[t];
+            if(tl.phase > 0)
+            {
+               const int k = tl.mesh * a.nphase + tl.phase - 1, need = a.need[k];
+               volatile int *dp = a.done + k;
+               int it = 0;
+               while(*dp < need)
+               {
+                  if(++it > BQ_SPIN || *(volatile int *)a.abort)
+                  {
+                     atomicOr(a.err, 16);
+                     *(volatile int *)a.abort = 1;
+                     t = -1;
+                     break;
+                  }
+                  __nanosleep(256);
+               }
+               __threadfence();
+            }
+         }
+      }
+      t = __shfl_sync(0xffffffffu, t, 0);
+      if(t < 0)
+         break;
+      const GmdBatchTile tl = a.tiles[t];
+      const GmdBatchMesh m = a.mesh[tl.mesh];
+      if(tl.phase < a.nsweep)
+      {
+         const float4 *in = (tl.phase & 1) ? b1 : b0;
+         float4 *out = (tl.phase & 1) ? b0 : b1;
+         warp_sweep_slices(tl.beg, tl.end, a.rowv, a.soff, a.col, in, out, a.omega);
+      }
+      else
+      {
+         const float4 *crd = (a.nsweep & 1) ? b1 : b0;
+         warp_quality_range(tl.beg, tl.end, (const int4 *)a.tet + m.t0, crd, m.thr, a.flags + m.f0,
+                            acc, hist);
+         warp_flush(acc, hist, a.stats + tl.mesh);
+      }
+      /* the warp's writes are visible at GPU scope before the tile counts */
+      __threadfence();
+      __syncwarp();
+      if(lane == 0)
+         atomicAdd(a.done + tl.mesh * a.nphase + tl.phase, 1);
+   }
+}
+
+extern "C" int gmd_batch_queue_warp(GmdCtx *ctx, const GmdBatchArgs *a, int grid)
+{
+   cudaStream_t s = (cudaStream_t)gmd_stream(ctx);
+   batch_warp_kernel<<<grid, MK_THREADS, 0, s>>>(*a);
+   return cudaGetLastError() == cudaSuccess;
+}
+
 extern "C" int gmd_batch_queue(GmdCtx *ctx, const GmdBatchArgs *a, int grid)
 {
    cudaStream_t s = (cudaStream_t)gmd_stream(ctx);

@@ -239,11 +239,18 @@ int      GmlxBatchRun         (size_t, int nsweeps, float omega, int mode, GmlxQ
 int      GmlxBatchGetMesh     (size_t, int MshIdx, float *crd);
 int      GmlxBatchFlags       (size_t, int MshIdx, unsigned *flags, size_t nwords);
 
-/* Time the queue on the packed meshes with several tile and grid sizes and
-   keep the fastest (the coordinates are restored afterwards); read back
-   the choice and the tile count. */
+/* Time the queue on the packed meshes with tiles claimed per block or per
+   warp, several tile sizes and grid sizes, and keep the fastest (the
+   coordinates are restored afterwards); read back the choice (WarpTiles 1:
+   per-warp tiles) and the tile count. */
 int      GmlxBatchTune        (size_t, int nsweeps, float omega);
-int      GmlxBatchInfo        (size_t, int *TileSlices, int *TileTets, int *grid, int *ntile);
+
+/* Set the queue's configuration by hand: tiles per warp (1) or per block
+   (0), slices per sweep tile, tets per quality tile (a multiple of 32),
+   grid (0: keep). */
+int      GmlxBatchSetTiles    (size_t, int WarpTiles, int TileSlices, int TileTets, int grid);
+int      GmlxBatchInfo        (size_t, int *TileSlices, int *TileTets, int *grid, int *ntile,
+                               int *WarpTiles);
 
 /* ---------------------------------------------------------------------------
  * Request loop: quality, smoothing and solve requests on registered meshes

@@ -75,12 +75,15 @@ def same_quality(a, b):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", [G.GmlxBatchQueue, G.GmlxBatchLoop])
+@pytest.mark.parametrize("mode,warp", [(G.GmlxBatchQueue, 0), (G.GmlxBatchQueue, 1),
+                                       (G.GmlxBatchLoop, 0)])
 @pytest.mark.parametrize("sweeps", [0, 3])
-def test_batch_matches_each_mesh_alone(mode, sweeps):
+def test_batch_matches_each_mesh_alone(mode, warp, sweeps):
     ms = meshes()
     g = make_batch(ms)
     try:
+        if warp:
+            assert G.lib.GmlxBatchSetTiles(g, 1, 4, 1024, 0) == 1
         res = (G.GmlxQuality * len(ms))()
         assert G.lib.GmlxBatchRun(g, sweeps, OMEGA, mode, res) == 1
         got = batch_results(g, ms)
@@ -106,10 +109,10 @@ def test_batch_replay_and_tuning_keep_results():
         after = batch_results(g, ms)
         for a, b in zip(before, after):
             assert np.array_equal(a[0], b[0])
-        ts, tt, grid, nt = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ts, tt, grid, nt, wt = (ctypes.c_int() for _ in range(5))
         assert G.lib.GmlxBatchInfo(g, ctypes.byref(ts), ctypes.byref(tt), ctypes.byref(grid),
-                                   ctypes.byref(nt)) == 1
-        assert ts.value in (8, 32, 128) and grid.value > 0
+                                   ctypes.byref(nt), ctypes.byref(wt)) == 1
+        assert ts.value in (2, 4, 8, 16, 32, 128) and grid.value > 0 and wt.value in (0, 1)
         res = (G.GmlxQuality * len(ms))()
         for _ in range(2):
             assert G.lib.GmlxBatchRun(g, 2, OMEGA, G.GmlxBatchQueue, res) == 1
