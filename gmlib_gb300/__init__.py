@@ -156,6 +156,9 @@ SIGNATURES.update({
     "GmlxSolveCG": (_i, [_s, _i, _i, _i, _i, _d, _i, ctypes.POINTER(GmlxSolveInfo)]),
     "GmlxCubeSpdSizes": (_i, [_i, _i, _ip, _ip]),
     "GmlxVectorData": (_i, [_s, _i]),
+    "GmlxImportMesh": (_i, [_s, _cp, _i, _ip]),
+    "GmlxExportMesh": (_i, [_s, _cp, _i, _ip]),
+    "GmlxExportSolution": (_i, [_s, _cp, _i, _ip]),
     "GmlxBatchCreate": (_i, [_s, _i, _p, _p, _p]),
     "GmlxBatchSetMesh": (_i, [_s, _i, _p, _p, _p]),
     "GmlxBatchSetup": (_i, [_s, _i]),

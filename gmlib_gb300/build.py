@@ -27,7 +27,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 C_SOURCES = ["gmlib3.c", "gml_tables.c", "gml_topo.c", "gml_codegen.c",
              "gml_dialect.c", "gml_ext.c", "gml_native.c", "gml_linalg.c",
              "gml_solver.c", "gml_problem.c", "gml_batch.c", "gml_serve.c",
-             "gml_hostcopy.c"]
+             "gml_hostcopy.c", "gml_meshio.c"]
 CU_SOURCES = ["gml_device.cu", "gml_reduce.cu", "gml_linalg_kernels.cu",
               "gml_mesh_kernels.cu", "gml_solver_kernels.cu", "gml_scan.cu"]
 EMBEDDED = ["gml_cl.h", "gml_toolkit.h"]

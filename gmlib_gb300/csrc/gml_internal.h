@@ -141,6 +141,7 @@ extern const int   GmlItmNmbEdg[8];
 extern const int   GmlItmNmbFac[8];
 extern const int   GmlItmEdgNod[8][12][2];
 extern const int   GmlItmFacNod[8][6][4];
+extern const int   GmlItmFacDeg[8][6];
 extern const int   GmlOclVecPow[5];
 
 /* gmlib3.c internals shared with the other host files */

@@ -82,6 +82,11 @@ const int GmlItmNmbVer[8] = {1,2,3,4,4,5,6,8};
 const int GmlItmNmbEdg[8] = {0,1,3,4,6,8,9,12};
 const int GmlItmNmbFac[8] = {0,0,1,1,4,5,5,6};
 
+/* vertex count of each element face (3 triangle, 4 quadrilateral) */
+const int GmlItmFacDeg[8][6] = {
+{0,0,0,0,0,0}, {0,0,0,0,0,0}, {3,0,0,0,0,0}, {4,0,0,0,0,0},
+{3,3,3,3,0,0}, {3,3,3,3,4,0}, {3,3,4,4,4,0}, {4,4,4,4,4,4} };
+
 /* local node pairs of each element edge */
 const int GmlItmEdgNod[8][12][2] = {
 { {0,0},{0,0},{0,0},{0,0},{0,0},{0,0},{0,0},{0,0},{0,0},{0,0},{0,0},{0,0} },

@@ -532,6 +532,119 @@ int GmlExtractEdges(size_t GmlIdx)
 }
 
 /* ------------------------------------------------------------------------- */
+/* GmlExtractFaces (reference sources/gmlib3.c:3880-4171)                     */
+/* ------------------------------------------------------------------------- */
+
+/* Every distinct triangle and quadrilateral face of the mesh.  Faces are
+   visited in the reference's order: existing triangles, existing
+   quadrilaterals, then the faces of tetrahedra, pyramids, prisms and
+   hexahedra, element by element and face by face; the first visit of a
+   node set defines the face.  As in the reference the face's nodes are
+   stored sorted (GetItmNod sorts them for hashing), existing surface faces
+   keep their reference and new faces get 0.  The triangle and quadrilateral
+   datatypes are replaced by the extracted ones.  Returns the number of
+   triangles plus quadrilaterals.  Deviation: the reference gives an
+   existing quadrilateral its fourth node as reference (QadTab[i][3],
+   :4093); here it keeps its reference. */
+static int faces_to_datatype(GmlSct *gml, size_t GmlIdx, int typ, const int *tab, const int *ref,
+                             int n)
+{
+   const int nn = typ == GmlTriangles ? 3 : 4;
+   int idx, *row, *rt, w;
+   GmlDatSct *d;
+   if(gml->TypIdx[typ])
+   {
+      int old = gml->TypIdx[typ];
+      GmlFreeData(GmlIdx, gml->RefIdx[typ]);
+      GmlFreeData(GmlIdx, old);
+      gml->TypIdx[typ] = gml->RefIdx[typ] = 0;
+   }
+   if(!n)
+      return 1;
+   if(!(idx = GmlNewMeshData(GmlIdx, typ, n)))
+      return 0;
+   d = &gml->dat[idx];
+   w = GmlTypVecSiz[ d->ItmTyp ];
+   row = (int *)d->CpuMem;
+   rt = (int *)gml->dat[ gml->RefIdx[typ] ].CpuMem;
+   for(int i=0;i<n;i++)
+   {
+      for(int c=0;c<w;c++)
+         row[(size_t)i * w + c] = c < nn ? tab[(size_t)i * nn + c] : 0;
+      rt[i] = ref[i];
+   }
+   return gml_upload(gml, idx) && gml_upload(gml, gml->RefIdx[typ]);
+}
+
+int GmlExtractFaces(size_t GmlIdx)
+{
+   GETGMLPTR(gml, GmlIdx);
+   size_t cap[2] = { 0, 0 };
+   int n[2] = { 0, 0 }, *tab[2] = { NULL, NULL }, *ref[2] = { NULL, NULL }, ok = 0;
+   TupMap map[2];
+   int have[2] = { 0, 0 };
+
+   for(int typ=GmlTriangles;typ<GmlMaxEleTyp;typ++)
+      if(gml->TypIdx[typ])
+         for(int j=0;j<GmlItmNmbFac[typ];j++)
+            cap[ GmlItmFacDeg[typ][j] == 4 ] += (size_t)gml->dat[ gml->TypIdx[typ] ].NmbLin;
+
+   for(int k=0;k<2;k++)
+   {
+      const int len = k ? 4 : 3;
+      if(!cap[k])
+         continue;
+      if(!tup_init(&map[k], len, cap[k]))
+         goto done;
+      have[k] = 1;
+      tab[k] = malloc(cap[k] * len * sizeof(int));
+      ref[k] = malloc(cap[k] * sizeof(int));
+      if(!tab[k] || !ref[k])
+         goto done;
+   }
+
+   for(int typ=GmlTriangles;typ<GmlMaxEleTyp;typ++)
+   {
+      GmlDatSct *d;
+      const int *nod, *rt;
+      int w;
+      if(!gml->TypIdx[typ])
+         continue;
+      d = &gml->dat[ gml->TypIdx[typ] ];
+      gml_wait_upload(gml, d);
+      nod = (const int *)d->CpuMem;
+      rt = (const int *)gml->dat[ gml->RefIdx[typ] ].CpuMem;
+      w = GmlTypVecSiz[ d->ItmTyp ];
+      for(int i=0;i<d->NmbLin;i++)
+         for(int j=0;j<GmlItmNmbFac[typ];j++)
+         {
+            const int k = GmlItmFacDeg[typ][j] == 4, len = k ? 4 : 3;
+            int t[4];
+            item_nodes(nod + (size_t)i * w, typ, k ? GmlQuadrilaterals : GmlTriangles, j, t);
+            if(tup_get_or_put(&map[k], t, n[k]) < 0)
+            {
+               memcpy(tab[k] + (size_t)n[k] * len, t, len * sizeof(int));
+               ref[k][ n[k] ] = (typ == GmlTriangles || typ == GmlQuadrilaterals) && rt ? rt[i] : 0;
+               n[k]++;
+            }
+         }
+   }
+
+   ok = faces_to_datatype(gml, GmlIdx, GmlTriangles, tab[0], ref[0], n[0])
+     && faces_to_datatype(gml, GmlIdx, GmlQuadrilaterals, tab[1], ref[1], n[1]);
+
+done:
+   for(int k=0;k<2;k++)
+   {
+      if(have[k])
+         tup_free(&map[k]);
+      free(tab[k]);
+      free(ref[k]);
+   }
+   return ok ? n[0] + n[1] : 0;
+}
+
+/* ------------------------------------------------------------------------- */
 /* GmlSetNeighbours (reference sources/gmlib3.c:4178-4267)                    */
 /* ------------------------------------------------------------------------- */
 

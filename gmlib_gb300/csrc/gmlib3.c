@@ -1630,9 +1630,3 @@ float GmlEvaluateNumbering(size_t GmlIdx)
 
 /* Face extraction is not part of the GB300 path (no configuration uses it);
    the entry point exists so that existing programs link, and reports it. */
-int GmlExtractFaces(size_t GmlIdx)
-{
-   (void)GmlIdx;
-   puts("GmlExtractFaces is not available in this build.");
-   return 0;
-}

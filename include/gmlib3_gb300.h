@@ -349,6 +349,28 @@ int      GmlxCubeSpdMatrix    (int n, int split, uint64_t seed, int *lin, int *c
                                double *val, double *rhs);
 
 /* ---------------------------------------------------------------------------
+ * Mesh files without libMeshb.  GmlImportMesh / GmlExportSolution (declared
+ * in gmlib3.h under WITH_LIBMESHB as in the reference, gmlib3.c:4480-4738)
+ * are always provided, on the library's own reader and writer of the Gamma
+ * mesh format (.meshb binary versions 1-4, .mesh ASCII).  These are their
+ * non-variadic forms plus a mesh writer.
+ * ------------------------------------------------------------------------- */
+
+/* Read the keywords of KwdTab (libMeshb codes: Vertices 4, Edges 5,
+   Triangles 6, Quadrilaterals 7, Tetrahedra 8, Prisms 9, Hexahedra 10,
+   Pyramids 49) and create their mesh datatypes.  Returns NmbKwd, 0 when the
+   file cannot be read. */
+int      GmlxImportMesh       (size_t, const char *MshNam, int NmbKwd, const int *KwdTab);
+
+/* Write the mesh types of TypTab (GmlVertices ...) to a .meshb (binary
+   version 2) or .mesh (ASCII) file.  Returns 1. */
+int      GmlxExportMesh       (size_t, const char *MshNam, int NmbTyp, const int *TypTab);
+
+/* Write float datatypes as ASCII solution fields (.sol), one SolAt keyword
+   per mesh type.  Returns the number of keywords written. */
+int      GmlxExportSolution   (size_t, const char *SolNam, int NmbDat, const int *DatTab);
+
+/* ---------------------------------------------------------------------------
  * Synthetic meshes and renumbering (host utilities).  No counterpart in the
  * reference library; the reference renumbers meshes with an external Hilbert
  * tool (README.md, todolist.md:44).

@@ -257,3 +257,51 @@ def cg(lin, col, val, rhs, tol, maxit):
     it = lib().orc_cg(nrow, b, _ptr(lin), _ptr(col), _ptr(val), _ptr(rhs), _ptr(x),
                       float(tol), int(maxit))
     return x, it
+
+
+# ------------------------------------------------------------ face extraction
+
+# local face nodes and face sizes per element type (sources/gmlib3.c:342-358)
+FACE_NODES = {
+    2: [(0, 1, 2)],
+    3: [(0, 1, 2, 3)],
+    4: [(1, 2, 3), (2, 0, 3), (3, 0, 1), (0, 2, 1)],
+    5: [(0, 1, 4), (1, 2, 4), (2, 3, 4), (3, 0, 4), (3, 2, 1, 0)],
+    6: [(0, 2, 1), (3, 4, 5), (0, 1, 4, 3), (1, 2, 5, 4), (3, 5, 2, 0)],
+    7: [(0, 4, 7, 3), (1, 2, 6, 5), (0, 1, 5, 4), (3, 7, 6, 2), (0, 3, 2, 1), (4, 5, 6, 7)],
+}
+
+
+def extract_faces(elements, quad_ref_quirk=False):
+    """Restatement of GmlExtractFaces (sources/gmlib3.c:3880-4171), pure
+    Python for small meshes.  elements: {type: (nodes [n, k], refs [n])}
+    for types 2 (triangles) .. 7 (hexahedra).  Faces are visited type by
+    type, element by element, face by face; the first visit of a sorted
+    node tuple defines the face (sorted nodes, the element's reference for
+    existing triangles / quadrilaterals, 0 otherwise).  With quad_ref_quirk
+    an existing quadrilateral gets its fourth node as reference, as the
+    reference code does (:4093).  Returns (triangles [n, 4], quads [n, 5])
+    with the reference in the last column."""
+    seen = [dict(), dict()]
+    out = [[], []]
+    for typ in range(2, 8):
+        if typ not in elements:
+            continue
+        nodes, refs = elements[typ]
+        for i in range(len(nodes)):
+            for loc in FACE_NODES[typ]:
+                key = tuple(sorted(int(nodes[i][c]) for c in loc))
+                k = len(key) == 4
+                if key in seen[k]:
+                    continue
+                seen[k][key] = len(out[k])
+                if typ in (2, 3):
+                    r = int(refs[i])
+                    if k and quad_ref_quirk:
+                        r = int(nodes[i][3])
+                else:
+                    r = 0
+                out[k].append(list(key) + [r])
+    tri = np.array(out[0], np.int32).reshape(-1, 4)
+    qad = np.array(out[1], np.int32).reshape(-1, 5)
+    return tri, qad
