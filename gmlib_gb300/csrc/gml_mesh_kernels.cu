@@ -1131,7 +1131,7 @@ __device__ __forceinline__ void batch_quality_range(int beg, int end, const int4
    }
 }
 
-__global__ void __launch_bounds__(MK_THREADS)
+__global__ void __launch_bounds__(MK_THREADS, 5)
 batch_queue_kernel(GmdBatchArgs a)
 {
    __shared__ int s_tile;
@@ -1345,7 +1345,7 @@ __device__ __forceinline__ void warp_flush(QAcc &a, unsigned *hist, GmlxQualStat
    a = QAcc{ 3.402823466e38f, -3.402823466e38f, 0.f, 0.f, -1, -1, 0u, 0u };
 }
 
-__global__ void __launch_bounds__(MK_THREADS)
+__global__ void __launch_bounds__(MK_THREADS, 5)
 batch_warp_kernel(GmdBatchArgs a)
 {
    __shared__ unsigned hist_all[MK_THREADS / 32][64];
