@@ -48,6 +48,8 @@ typedef struct
    GmdSvScal   *sc, *hsc;        /* device scalars, pinned host copies (2 slots) */
    void        *g64, *g32;       /* graphs of GML_CG_CHUNK iterations */
    void        *ev[2], *t0, *t1;
+   void        *tr[4];           /* phase and kernel timing of GML_CG_TRACE */
+   int         chunk;            /* iterations per replay of g64 / g32 */
 }GmlSolver;
 
 static double inner_factor(void)
@@ -55,6 +57,14 @@ static double inner_factor(void)
    const char *e = getenv("GML_CG_INNER");
    double f = e ? atof(e) : 0.;
    return f > 0. && f < 1. ? f : 1e-5;
+}
+
+/* iterations per graph replay (GML_CG_CHUNK overrides, 1..64) */
+static int cg_chunk(void)
+{
+   const char *e = getenv("GML_CG_CHUNK");
+   int c = e ? atoi(e) : 0;
+   return c >= 1 && c <= 64 ? c : GML_CG_CHUNK;
 }
 
 static void solver_free(GmlSct *gml, GmlSolver *s)
@@ -74,6 +84,8 @@ static void solver_free(GmlSct *gml, GmlSolver *s)
       gmd_event_free(s->ev[i]);
    gmd_event_free(s->t0);
    gmd_event_free(s->t1);
+   for(int i=0;i<4;i++)
+      gmd_event_free(s->tr[i]);
    free(s);
 }
 
@@ -112,9 +124,12 @@ static GmlSolver *solver_get(GmlSct *gml, GmlMatSct *mat, int mixed)
       s->ev[1] = gmd_event_new_sync();
       s->t0 = gmd_event_new();
       s->t1 = gmd_event_new();
+      for(int i=0;i<4;i++)
+         s->tr[i] = gmd_event_new();
+      s->chunk = cg_chunk();
       mat->Sol = s;
       if(!s->b64 || !s->x64 || !s->r64 || !s->part || !s->sc || !s->hsc
-      || !s->ev[0] || !s->ev[1] || !s->t0 || !s->t1)
+      || !s->ev[0] || !s->ev[1] || !s->t0 || !s->t1 || !s->tr[0] || !s->tr[1] || !s->tr[2] || !s->tr[3])
          return NULL;
    }
    if(!mixed && !s->p64)
@@ -161,19 +176,21 @@ static int capture(GmlSct *gml, GmlSolver *s, const GmlSellDev *A, int fs,
       return 1;
    if(!gmd_graph_begin(gml->dev))
       return 0;
-   for(int i=0;i<GML_CG_CHUNK && ok;i++)
+   for(int i=0;i<s->chunk && ok;i++)
       ok = cg_iteration(gml, s, A, fs, x, r, p, q);
    if(!gmd_graph_end(gml->dev, graph))
       return 0;
    return ok;
 }
 
+static int read_scalars(GmlSct *gml, GmlSolver *s, GmdSvScal *out);
+
 /* replay the iteration graph until the device stop flag is set; two replays
    are kept in flight, each followed by a copy of the scalars to its own
    pinned slot.  Returns the iterations done, or -1. */
 static int run_cg(GmlSct *gml, GmlSolver *s, void *graph, int maxit)
 {
-   int launched = 0, checked = 0, cap = maxit / GML_CG_CHUNK + 2;
+   int launched = 0, checked = 0, cap = maxit / s->chunk + 2;
    for(;;)
    {
       while(launched < cap && launched - checked < 2)
@@ -206,6 +223,66 @@ static int run_cg(GmlSct *gml, GmlSolver *s, void *graph, int maxit)
    }
 }
 
+/* GML_CG_TRACE=1 prints the wall and device time of each phase of a solve
+   (stderr); GML_CG_TRACE=2 also runs the iterations one kernel at a time
+   without graphs and prints each kernel's mean device time */
+static int trace_on(void)
+{
+   static int on = -1;
+   if(on < 0)
+   {
+      const char *e = getenv("GML_CG_TRACE");
+      on = e && (*e == '1' || *e == '2') ? *e - '0' : 0;
+   }
+   return on;
+}
+
+/* the iterations of run_cg, launched one by one with an event between the
+   kernels; synchronises after each iteration */
+static int run_cg_timed(GmlSct *gml, GmlSolver *s, const GmlSellDev *A, int fs,
+                        void *x, void *r, void *p, void *q, int maxit)
+{
+   double t[3] = {0., 0., 0.};
+   int n = 0;
+   GmdSvScal h;
+   for(;;)
+   {
+      if(!gmd_event_record(gml->dev, s->tr[0])
+      || !gmd_sv_spmv_dot(gml->dev, A, p, q, s->part, s->sc)
+      || !gmd_event_record(gml->dev, s->tr[1])
+      || !gmd_sv_update(gml->dev, fs, s->n, x, r, p, q, s->part, s->sc)
+      || !gmd_event_record(gml->dev, s->tr[2])
+      || !gmd_sv_dir(gml->dev, fs, s->n, p, r, s->sc)
+      || !gmd_event_record(gml->dev, s->tr[3])
+      || !read_scalars(gml, s, &h))
+         return -1;
+      for(int k=0;k<3;k++)
+         t[k] += gmd_event_elapsed_s(s->tr[k], s->tr[k+1]);
+      n++;
+      if(h.done || n > maxit)
+         break;
+   }
+   fprintf(stderr, "cg kernels fp%d: spmv_dot %.1f us  update %.1f us  dir %.1f us  (%d launches each)\n",
+           8 * fs, 1e6 * t[0] / n, 1e6 * t[1] / n, 1e6 * t[2] / n, n);
+   return h.done == 1 ? h.it : h.done == 2 ? -2 : -1;
+}
+
+/* wall and device time of the phase that ends here; the device time runs
+   from the previous trace point (events on the instance's stream) */
+static void trace(GmlSct *gml, GmlSolver *s, const char *what, double *t, int it)
+{
+   double now, dev;
+   if(!trace_on())
+      return;
+   gmd_event_record(gml->dev, s->tr[1]);
+   dev = gmd_event_elapsed_s(s->tr[0], s->tr[1]);
+   now = GmlGetWallClock();
+   fprintf(stderr, "cg %-10s %8.3f ms wall %8.3f ms device  it %d  chunk %d\n", what,
+           1e3 * (now - *t), 1e3 * dev, it, s->chunk);
+   *t = now;
+   gmd_event_record(gml->dev, s->tr[0]);
+}
+
 static int read_scalars(GmlSct *gml, GmlSolver *s, GmdSvScal *out)
 {
    if(!gmd_d2h_async(gml->dev, &s->hsc[0], s->sc, sizeof(GmdSvScal)) || !gmd_sync(gml->dev))
@@ -224,7 +301,7 @@ int GmlxSolveCG(size_t GmlIdx, int MatIdx, int RhsIdx, int SolIdx, int mode, dou
    GmlSolver *s;
    GmdSvScal h;
    int it = 0, out = 0, r;
-   double tin;
+   double tin, tt = GmlGetWallClock();
 
    if(info)
       memset(info, 0, sizeof(GmlxSolveInfo));
@@ -262,6 +339,8 @@ int GmlxSolveCG(size_t GmlIdx, int MatIdx, int RhsIdx, int SolIdx, int mode, dou
    if(rv->NmbValTyp * rv->VecValSiz != s->vs || sv->NmbValTyp * sv->VecValSiz != s->vs)
       return -3;
    gmd_event_record(gml->dev, s->t0);
+   if(trace_on())
+      gmd_event_record(gml->dev, s->tr[0]);
 
    if(mode == GmlxCgFp64)
    {
@@ -269,7 +348,9 @@ int GmlxSolveCG(size_t GmlIdx, int MatIdx, int RhsIdx, int SolIdx, int mode, dou
                       8, s->part, s->sc, tol * tol, MaxIte)
       || !capture(gml, s, A, 8, s->x64, s->r64, s->p64, s->q64, &s->g64))
          return -6;
-      r = run_cg(gml, s, s->g64, MaxIte);
+      r = trace_on() == 2 ? run_cg_timed(gml, s, A, 8, s->x64, s->r64, s->p64, s->q64, MaxIte)
+                          : run_cg(gml, s, s->g64, MaxIte);
+      trace(gml, s, "fp64 cg", &tt, r);
       if(r < 0)
       {
          printf("CG failed (%s)\n", r == -2 ? "p.Ap <= 0: matrix not positive definite" : "device");
@@ -289,12 +370,16 @@ int GmlxSolveCG(size_t GmlIdx, int MatIdx, int RhsIdx, int SolIdx, int mode, dou
          return -6;
       if(!read_scalars(gml, s, &h))
          return -6;
+      trace(gml, s, "init", &tt, 0);
       while(h.rt > tol * tol * h.bb && out < GML_CG_MAXOUT && it < MaxIte)
       {
          if(!gmd_sv_ir_begin(gml->dev, s->n, s->r64, s->r32, s->p32, s->d32, s->part, s->sc,
                              tin * tin, MaxIte - it))
             return -6;
-         r = run_cg(gml, s, s->g32, MaxIte - it);
+         r = trace_on() == 2
+           ? run_cg_timed(gml, s, &s->A32, 4, s->d32, s->r32, s->p32, s->q32, MaxIte - it)
+           : run_cg(gml, s, s->g32, MaxIte - it);
+         trace(gml, s, "fp32 cg", &tt, r);
          if(r < 0)
          {
             printf("CG failed (%s)\n", r == -2 ? "p.Ap <= 0: matrix not positive definite" : "device");
@@ -306,6 +391,7 @@ int GmlxSolveCG(size_t GmlIdx, int MatIdx, int RhsIdx, int SolIdx, int mode, dou
          || !gmd_sv_residual(gml->dev, A, s->b64, s->x64, s->r64, s->part, s->sc)
          || !read_scalars(gml, s, &h))
             return -6;
+         trace(gml, s, "residual", &tt, 0);
       }
    }
 

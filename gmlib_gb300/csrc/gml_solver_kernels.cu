@@ -111,15 +111,40 @@ template<class T> __device__ __forceinline__ T lane(const typename Vec16<T>::typ
    return reinterpret_cast<const T *>(&v)[i];
 }
 
-template<class T> __device__ __forceinline__ double dot16(const typename Vec16<T>::type &a,
-                                                          const typename Vec16<T>::type &b)
+/* dot of two 16-byte chunks in their own precision */
+template<class T> __device__ __forceinline__ T dot16(const typename Vec16<T>::type &a,
+                                                     const typename Vec16<T>::type &b)
 {
-   double s = 0.;
+   T s = (T)0;
 #pragma unroll
    for(int i=0;i<Vec16<T>::n;i++)
-      s += (double)lane<T>(a, i) * (double)lane<T>(b, i);
+      s = fma(lane<T>(a, i), lane<T>(b, i), s);
    return s;
 }
+
+/* per-thread dot accumulator.  FP64 vectors add in FP64.  FP32 vectors add
+   into an error-free TwoSum pair in FP32 and convert once at the end: a
+   conversion and an FP64 add per element would put the FP64 pipe, a small
+   fraction of the FP32 rate on this part, on the per-element path (it made
+   the FP32 SpMV and update kernels 25-50 % slower than their memory time). */
+template<class T> struct SvAcc;
+template<> struct SvAcc<double>
+{
+   double s = 0.;
+   __device__ __forceinline__ void add(double v) { s += v; }
+   __device__ __forceinline__ double get() const { return s; }
+};
+template<> struct SvAcc<float>
+{
+   float s = 0.f, c = 0.f;
+   __device__ __forceinline__ void add(float v)
+   {
+      const float t = s + v, bp = t - s;
+      c += (s - (t - bp)) + (v - bp);
+      s = t;
+   }
+   __device__ __forceinline__ double get() const { return (double)s + (double)c; }
+};
 
 template<class VT>
 __global__ void __launch_bounds__(SV_THREADS)
@@ -198,7 +223,8 @@ sv_spmv_dot_kernel(int nrow, const int64_t *__restrict__ soff, const int *__rest
 {
    typedef typename Vec16<T>::type V;
    constexpr int NV = VS / Vec16<T>::n;
-   double acc = 0., tot;
+   SvAcc<T> acc;
+   double tot;
    if(sv_stopped(sc))
       return;
    for(int r=blockIdx.x*blockDim.x+threadIdx.x;r<nrow;r+=gridDim.x*blockDim.x)
@@ -215,10 +241,10 @@ sv_spmv_dot_kernel(int nrow, const int64_t *__restrict__ soff, const int *__rest
          for(int i=0;i<Vec16<T>::n;i++)
             reinterpret_cast<T *>(&t)[i] = y[ u * Vec16<T>::n + i ];
          qp[u] = t;
-         acc += dot16<T>(__ldg(pp + u), t);
+         acc.add(dot16<T>(__ldg(pp + u), t));
       }
    }
-   if(sv_grid_sum(acc, part, sc, &tot))
+   if(sv_grid_sum(acc.get(), part, sc, &tot))
    {
       sc->pq = tot;
       if(tot > 0.)
@@ -238,7 +264,8 @@ sv_update_kernel(size_t n, T *__restrict__ x, T *__restrict__ r, const T *__rest
 {
    typedef typename Vec16<T>::type V;
    const size_t nv = n / Vec16<T>::n;
-   double acc = 0., tot;
+   SvAcc<T> acc;
+   double tot;
    if(sv_stopped(sc))
       return;
    const T a = (T)sc->alpha;
@@ -256,9 +283,9 @@ sv_update_kernel(size_t n, T *__restrict__ x, T *__restrict__ r, const T *__rest
       }
       xv[i] = xx;
       rv[i] = rr;
-      acc += dot16<T>(rr, rr);
+      acc.add(dot16<T>(rr, rr));
    }
-   if(sv_grid_sum(acc, part, sc, &tot))
+   if(sv_grid_sum(acc.get(), part, sc, &tot))
    {
       sc->beta = tot / sc->rr;
       sc->rr = tot;
@@ -319,7 +346,8 @@ sv_ir_begin_kernel(size_t n, const double *__restrict__ r64, float *__restrict__
                    float *__restrict__ p32, float *__restrict__ d32, double *part,
                    GmdSvScal *sc, double tin2, int maxit)
 {
-   double acc = 0., tot;
+   SvAcc<float> acc;
+   double tot;
    const double rt = sc->rt;
    const double s = rt > 0. ? 1.0 / sqrt(rt) : 0.;
    for(size_t i=(size_t)blockIdx.x*blockDim.x+threadIdx.x;i<n;i+=(size_t)gridDim.x*blockDim.x)
@@ -328,9 +356,9 @@ sv_ir_begin_kernel(size_t n, const double *__restrict__ r64, float *__restrict__
       r32[i] = v;
       p32[i] = v;
       d32[i] = 0.f;
-      acc += (double)v * (double)v;
+      acc.add(v * v);
    }
-   if(sv_grid_sum(acc, part, sc, &tot))
+   if(sv_grid_sum(acc.get(), part, sc, &tot))
    {
       sc->rr = tot;
       sc->stop = tin2 * tot;
@@ -365,13 +393,41 @@ static int sv_ok(void)
    return cudaGetLastError() == cudaSuccess;
 }
 
-/* flat kernels: 8 blocks per SM, grid-stride */
-static unsigned sv_flat_grid(GmdCtx *ctx, size_t n)
+/* resident blocks per SM of a kernel at SV_THREADS threads (8 if the query
+   fails) */
+static int sv_occupancy(const void *fn)
 {
-   size_t g = (n + SV_THREADS - 1) / SV_THREADS, cap = 8 * (size_t)gmd_num_sms(ctx);
+   int per = 0;
+   if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, SV_THREADS, 0) != cudaSuccess
+   || per < 1)
+   {
+      cudaGetLastError();
+      per = 8;
+   }
+   return per;
+}
+
+/* flat kernels: grid-stride over one wave of resident blocks (per = blocks
+   per SM), so that no second partial wave leaves SMs idle */
+static unsigned sv_flat_grid(GmdCtx *ctx, size_t n, int per = 8)
+{
+   size_t g = (n + SV_THREADS - 1) / SV_THREADS, cap = (size_t)per * gmd_num_sms(ctx);
    if(g > cap) g = cap;
    if(g > GMD_SV_MAXBLK) g = GMD_SV_MAXBLK;
    return (unsigned)(g ? g : 1);
+}
+
+/* the occupancy of each iteration kernel, queried once (thread-safe statics) */
+template<class T> static int sv_update_occ(void)
+{
+   static const int per = sv_occupancy((const void *)sv_update_kernel<T>);
+   return per;
+}
+
+template<class T> static int sv_dir_occ(void)
+{
+   static const int per = sv_occupancy((const void *)sv_dir_kernel<T>);
+   return per;
 }
 
 /* row kernels: one thread per block row */
@@ -439,10 +495,10 @@ extern "C" int gmd_sv_update(GmdCtx *ctx, int fltsiz, size_t n, void *x, void *r
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
    if(fltsiz == 8)
-      sv_update_kernel<double><<<sv_flat_grid(ctx, n / 2), SV_THREADS, 0, st>>>(n, (double *)x,
+      sv_update_kernel<double><<<sv_flat_grid(ctx, n / 2, sv_update_occ<double>()), SV_THREADS, 0, st>>>(n, (double *)x,
          (double *)r, (const double *)p, (const double *)q, part, sc);
    else
-      sv_update_kernel<float><<<sv_flat_grid(ctx, n / 4), SV_THREADS, 0, st>>>(n, (float *)x,
+      sv_update_kernel<float><<<sv_flat_grid(ctx, n / 4, sv_update_occ<float>()), SV_THREADS, 0, st>>>(n, (float *)x,
          (float *)r, (const float *)p, (const float *)q, part, sc);
    return sv_ok();
 }
@@ -452,10 +508,10 @@ extern "C" int gmd_sv_dir(GmdCtx *ctx, int fltsiz, size_t n, void *p, const void
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
    if(fltsiz == 8)
-      sv_dir_kernel<double><<<sv_flat_grid(ctx, n / 2), SV_THREADS, 0, st>>>(n, (double *)p,
+      sv_dir_kernel<double><<<sv_flat_grid(ctx, n / 2, sv_dir_occ<double>()), SV_THREADS, 0, st>>>(n, (double *)p,
          (const double *)r, sc);
    else
-      sv_dir_kernel<float><<<sv_flat_grid(ctx, n / 4), SV_THREADS, 0, st>>>(n, (float *)p,
+      sv_dir_kernel<float><<<sv_flat_grid(ctx, n / 4, sv_dir_occ<float>()), SV_THREADS, 0, st>>>(n, (float *)p,
          (const float *)r, sc);
    return sv_ok();
 }
