@@ -59,10 +59,12 @@ def parse():
     p.add_argument("--n", type=int, default=N_HEX, help="hexes per cube side")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=20)
-    p.add_argument("--workload", default="smooth", choices=["smooth", "solve", "batch", "serve"],
+    p.add_argument("--workload", default="smooth",
+                   choices=["smooth", "solve", "batch", "serve", "p2"],
                    help="smooth: the smoothing + quality step (default); solve: block SpMV "
                         "and CG; batch: 512 meshes through the tile queue vs the per-mesh "
-                        "launch loop; serve: the request loop on a Poisson stream")
+                        "launch loop; serve: the request loop on a Poisson stream; p2: the "
+                        "P2Quality flow through a generated kernel")
     p.add_argument("--meshes", type=int, default=512, help="batch: number of meshes")
     p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     p.add_argument("--rate", type=float, default=200.0, help="serve: requests per second")
@@ -479,6 +481,117 @@ def gen_meshes(specs):
         return list(ex.map(one, specs))
 
 
+# ------------------------------------------------------------- P2 quality
+
+P2_FLOPS = 1612.0          # flops per P2 tet, as counted by examples/P2Quality
+P2_PARAMS = b"typedef struct {\n   int   foo;\n   float res;\n}GmlParSct;\n"
+
+
+def run_p2(args, dist):
+    """The reference's P2Quality flow on the n^3-hex cube with quadratic tets
+    (Kuhn split, jitter 0.15h, mid-edge nodes moved by up to 0.05h): the
+    P2 quality body (gmlib_gb300/kernels/p2_quality.cl) compiled by
+    GmlCompileKernel, reading VerCrd through TetVer and MidCrd through the
+    tet -> edge downlink, one quality per tet.
+    value: P2 tet qualities per second, device time with CUDA events over K
+    launches, inputs resident (larger than L2); e2e: the same through the C
+    ABI with the vertex coordinates and mid-edge nodes uploaded and the
+    qualities downloaded every step."""
+    import gmlib_gb300 as G
+    n = args.n
+    t0 = time.perf_counter()
+    crd, tet, edges, mid, tedg = G.p2_mesh(n, split=0, jitter=0.15, curve=0.05, seed=SEED)
+    tgen = time.perf_counter() - t0
+    nv, nt, ne = len(crd), len(tet), len(edges)
+    g = G.lib.GmlInit(dist.local)
+    if not g:
+        raise SystemExit("GmlInit failed")
+    G.lib.GmlxSetTiming(g, 0)
+    G.lib.GmlNewParameters(g, len(P2_PARAMS), P2_PARAMS)
+    v, t, e, m = G.upload_p2(g, crd, tet, edges, mid)
+    q = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 1, G.GmlFlt, b"qal")
+    k = G.compile_kernel(g, G.p2_body(), "p2quality", G.GmlTetrahedra,
+                         [(v, G.GmlReadMode, 0), (m, G.GmlReadMode, 0), (q, G.GmlWriteMode, 0)])
+    if not k:
+        raise SystemExit("P2 kernel did not compile")
+    for _ in range(max(args.warmup, 3)):
+        if G.lib.GmlLaunchKernel(g, k) != 1:
+            raise SystemExit("launch failed")
+    G.lib.GmlxSynchronize(g)
+    e0, e1 = G.lib.GmlxEventCreate(), G.lib.GmlxEventCreate()
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    clocks.start()
+    time.sleep(0.3)
+    G.lib.GmlxEventRecord(g, e0)
+    for _ in range(args.steps):
+        G.lib.GmlLaunchKernel(g, k)
+    G.lib.GmlxEventRecord(g, e1)
+    dev_s = dist.max(G.lib.GmlxEventElapsed(e0, e1))
+    clk = clocks.stop()
+    per = dev_s / args.steps
+    qg = G.get_data(g, q, np.float32, nt)
+    sumq = G.reduce(g, q, G.GmlSum)
+    minq = G.reduce(g, q, G.GmlMin)
+    # algorithmic bytes of one launch: TetVer and the 6 used edge indices per
+    # tet, each vertex and mid-edge node once, the quality out
+    byts = 16.0 * nt + 24.0 * nt + 16.0 * nv + 16.0 * ne + 4.0 * nt
+    achieved = byts / per / 1e9
+    peak, peak_src = peak_hbm()
+
+    # end to end: coordinates and mid-edge nodes up, qualities down
+    host_crd, host_mid = np.ascontiguousarray(crd), np.ascontiguousarray(mid)
+    out = np.empty(nt, np.float32)
+    e2e_t = []
+    for i in range(args.e2e_steps + 2):
+        ts = time.perf_counter()
+        G.lib.GmlxSetData(g, v, G.as_ptr(host_crd), host_crd.nbytes)
+        G.lib.GmlxSetData(g, m, G.as_ptr(host_mid), host_mid.nbytes)
+        G.lib.GmlLaunchKernel(g, k)
+        G.lib.GmlxGetData(g, q, G.as_ptr(out), out.nbytes)
+        if i >= 2:
+            e2e_t.append(time.perf_counter() - ts)
+    e2e_s = dist.max(statistics.median(e2e_t))
+    G.lib.GmlStop(g)
+
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        import oracle as O
+        ns = min(nt, 2_000_000)
+        O.p2_quality(crd, mid, tet[:1000], tedg[:1000])        # warm the pool
+        ts = time.perf_counter()
+        O.p2_quality(crd, mid, tet[:ns], tedg[:ns])
+        tc = time.perf_counter() - ts
+        cpu = {"value": round(ns / tc / 1e6, 3), "unit": "M P2 tets/s",
+               "cores": os.cpu_count(), "kind": "port",
+               "sample": "FP64 oracle (OpenMP) on the first %d tets of the same mesh" % ns}
+    if dist.rank == 0:
+        line = {"metric": "P2 tet qualities per second", "value": round(dist.world * nt / per / 1e6, 2),
+                "unit": "M P2 tets/s", "n_gpus": dist.world, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": round(per * 1e3, 4),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "P2 tet quality (examples/P2Quality flow), %d^3-hex cube, "
+                                       "Kuhn split, curved mid-edge nodes" % n,
+                           "tets": nt, "vertices": nv, "edges": ne,
+                           "l2": "inputs larger than L2 (%.0f MB per launch)" % (byts / 1e6),
+                           "mesh_generation_s": round(tgen, 1)},
+                "gpu_launches": args.steps,
+                "roofline": {"bound": "hbm", "kernel": "p2quality (generated)",
+                             "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                             "frac": round(achieved / peak, 4), "traffic": None,
+                             "algorithmic_bytes_per_launch": byts,
+                             "gflops": round(P2_FLOPS * nt / per / 1e9, 1),
+                             "mean_launch_us": round(per * 1e6, 2), "peak_source": peak_src},
+                "e2e": {"value": round(dist.world * nt / e2e_s / 1e6, 2), "unit": "M P2 tets/s",
+                        "h2d_bytes_per_step": host_crd.nbytes + host_mid.nbytes,
+                        "d2h_bytes_per_step": out.nbytes, "ms_per_step": round(e2e_s * 1e3, 3)},
+                "cpu_baseline": cpu, "clocks": clk,
+                "result_check": {"mean_quality": sumq / nt, "min_quality": minq,
+                                 "min_matches_download": bool(minq == float(qg.min()))}}
+        print(json.dumps(line), flush=True)
+
+
 def run_batch(args, dist):
     """512 jittered tet cubes, hexes per side log-uniform in [10, 80], reflected
     split, Hilbert order: 5 sweeps + quality statistics (min/argmin) per mesh,
@@ -678,6 +791,8 @@ def main():
             run_batch(args, dist)
         elif args.workload == "serve":
             run_serve(args, dist)
+        elif args.workload == "p2":
+            run_p2(args, dist)
         else:
             run_gpu(args, dist)
     finally:

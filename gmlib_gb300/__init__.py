@@ -230,6 +230,38 @@ def cube_mesh(n, split=0, jitter=0.25, seed=12345, hilbert=True):
     return crd, tet, ref
 
 
+# local edges of a tetrahedron, in the order of the library's edge table
+TET_EDGES = ((0, 1), (1, 2), (2, 0), (3, 0), (3, 1), (3, 2))
+
+
+def p2_mesh(n, split=0, jitter=0.2, curve=0.15, seed=12345):
+    """Quadratic (P2) tetrahedra on the jittered n^3-hex cube: the unique
+    edges (ascending vertex pairs, sorted), one mid-edge node per edge (the
+    midpoint moved by up to curve * h in each coordinate, seeded) and the
+    tet -> edge table in TET_EDGES order.
+    Returns crd (nv,4), tet (nt,4), edges (ne,2), mid (ne,4), tedg (nt,6)."""
+    crd, tet, _ = cube_mesh(n, split=split, jitter=jitter, seed=seed)
+    nv = len(crd)
+    loc = np.array(TET_EDGES, np.int64)
+    a = tet[:, loc[:, 0]].astype(np.int64)
+    b = tet[:, loc[:, 1]].astype(np.int64)
+    key = np.minimum(a, b) * nv + np.maximum(a, b)
+    uniq, inv = np.unique(key.ravel(), return_inverse=True)
+    edges = np.stack([uniq // nv, uniq % nv], axis=1).astype(np.int32)
+    rng = np.random.default_rng(seed + 1)
+    mid = np.zeros((len(edges), 4), np.float32)
+    mid[:, :3] = 0.5 * (crd[edges[:, 0], :3] + crd[edges[:, 1], :3])
+    mid[:, :3] += (curve / n) * rng.uniform(-1.0, 1.0, (len(edges), 3)).astype(np.float32)
+    return crd, tet, edges, mid, inv.reshape(len(tet), 6).astype(np.int32)
+
+
+def p2_body():
+    """The P2 tetrahedron quality as a GMlib-dialect kernel body
+    (kernels/p2_quality.cl): reads VerCrd[4] and MidCrd[6..8], writes qal."""
+    with open(os.path.join(_HERE, "kernels", "p2_quality.cl"), "rb") as f:
+        return f.read()
+
+
 def compile_kernel(g, src, name, msh, dats):
     """dats: list of (index, flags, link) triplets."""
     n = len(dats)
@@ -298,6 +330,22 @@ def upload_mesh(g, crd, tet, ref=None):
     # keep the host arrays alive until the asynchronous upload is done
     lib.GmlxSynchronize(g)
     return vidx, tidx
+
+
+def upload_p2(g, crd, tet, edges, mid):
+    """The data of the reference's P2Quality example: vertices and tets,
+    the edges (GmlEdges lines) and the mid-edge nodes as an edge solution
+    named MidCrd.  Returns (vertex, tet, edge, MidCrd) indices."""
+    vidx, tidx = upload_mesh(g, crd, tet)
+    eidx = lib.GmlNewMeshData(g, GmlEdges, len(edges))
+    midx = lib.GmlNewSolutionData(g, GmlEdges, 1, GmlFlt4, b"MidCrd")
+    if not eidx or not midx:
+        raise RuntimeError("edge datatypes could not be created")
+    if not set_data(g, eidx, np.ascontiguousarray(edges, np.int32)) \
+       or not set_data(g, midx, np.ascontiguousarray(mid, np.float32)):
+        raise RuntimeError("edge upload failed")
+    lib.GmlxSynchronize(g)
+    return vidx, tidx, eidx, midx
 
 
 def reduce(g, idx, op):

@@ -175,6 +175,31 @@ def ref_gather(crd, deg, ball, opt):
     return crd, res
 
 
+def ref_p2_quality(crd, mid, tet, tedg):
+    """The reference's P2Quality body on the CPU (float32), or None."""
+    r = refcl()
+    if r is None:
+        return None
+    crd = np.ascontiguousarray(crd, np.float32)
+    mid = np.ascontiguousarray(mid, np.float32)
+    tet = np.ascontiguousarray(tet, np.int32)
+    tedg = np.ascontiguousarray(tedg, np.int32)
+    out = np.zeros(len(tet), np.float32)
+    r.ref_p2_quality(_ptr(crd), _ptr(mid), len(tet), _ptr(tet), _ptr(tedg), _ptr(out))
+    return out
+
+
+def p2_quality(crd, mid, tet, tedg):
+    """FP64 restatement of the P2 quality (orc_p2_quality)."""
+    crd = np.ascontiguousarray(crd, np.float32)
+    mid = np.ascontiguousarray(mid, np.float32)
+    tet = np.ascontiguousarray(tet, np.int32)
+    tedg = np.ascontiguousarray(tedg, np.int32)
+    q = np.zeros(len(tet), np.float64)
+    lib().orc_p2_quality(len(tet), _ptr(tet), _ptr(tedg), _ptr(crd), _ptr(mid), _ptr(q))
+    return q
+
+
 # ------------------------------------------------------ native mesh kernels
 
 def boundary_vertices(nv, tet):

@@ -2,7 +2,8 @@
 
   oracle/liboracle.so     the C restatement (oracle.c), gcc -O2 -fopenmp
   oracle/_ref/librefcl.so the reference's own kernel bodies and toolkit
-                          (sources/toolkit.cl, examples/*/ *.cl) compiled as
+                          (sources/toolkit.cl, examples/*/ *.cl, P2Quality
+                          included) compiled as
                           C++ against oracle/refcl/cl_host.h, from where they
                           lie in the reference tree; built only where that
                           tree exists (it is not shipped anywhere else).
@@ -58,7 +59,8 @@ def build_refcl(force=False):
             os.path.join(REF_ROOT, "sources", "toolkit.cl"),
             os.path.join(REF_ROOT, "examples", "MeshQuality", "compute_quality.cl"),
             os.path.join(REF_ROOT, "examples", "NodeSmoothing", "scatter.cl"),
-            os.path.join(REF_ROOT, "examples", "NodeSmoothing", "gather.cl")]
+            os.path.join(REF_ROOT, "examples", "NodeSmoothing", "gather.cl"),
+            os.path.join(REF_ROOT, "examples", "P2Quality", "quality.cl")]
     if force or _stale(REF_LIB, deps):
         _run(["g++", "-O2", "-fPIC", "-shared", "-fopenmp", "-std=c++17",
               "-fsingle-precision-constant", "-ffp-contract=off",

@@ -39,6 +39,10 @@ double orc_rel_residual(int nrow, int b, const int *lin, const int *col, const d
 int    orc_cg(int nrow, int b, const int *lin, const int *col, const double *val,
               const double *rhs, double *x, double tol, int maxit);
 
+double orc_p2_quality1(const double ver[4][3], const double mid[6][3]);
+void   orc_p2_quality(int nt, const int *tet, const int *tedg, const float *crd,
+                      const float *mid, double *q);
+
 #ifdef __cplusplus
 }
 #endif

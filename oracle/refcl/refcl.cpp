@@ -4,7 +4,7 @@
  * Test infrastructure.  Includes, from the reference tree (REF_ROOT), the
  * geometry toolkit (sources/toolkit.cl, found through -I) and the example kernel bodies
  * (examples/MeshQuality/compute_quality.cl, examples/NodeSmoothing/scatter.cl
- * and gather.cl), and wraps each body in the gather prologue and scatter
+ * and gather.cl, examples/P2Quality/quality.cl), and wraps each body in the gather prologue and scatter
  * epilogue that the reference's generator writes around it
  * (sources/gmlib3.c:2739-2938), one loop iteration per work-item.  Built with
  * -fsingle-precision-constant like the reference's OpenCL build
@@ -53,6 +53,34 @@ void ref_scatter(const float *crd, int nt, const int *tet, float *opt)
       for(int k=0;k<4;k++)
          for(int c=0;c<4;c++)
             opt[ 16 * (size_t)cnt + 4*k + c ] = OptCrd[k].v[c];
+   }
+}
+
+/* P2Quality: loop over tetrahedra, VerCrd[4] gathered through TetVer and
+   MidCrd[6] through the tetrahedron -> edge downlink TetEdg (6 edge lines
+   per tet in the local edge order of the edge table) */
+void ref_p2_quality(const float *crd, const float *mid, int nt, const int *tet,
+                    const int *tedg, float *out)
+{
+   #pragma omp parallel for schedule(static)
+   for(int cnt=0;cnt<nt;cnt++)
+   {
+      float4 VerCrd[4], MidCrd[6];
+      float qal;
+      for(int k=0;k<4;k++)
+      {
+         const float *c = &crd[ 4 * (size_t)tet[ 4*(size_t)cnt + k ] ];
+         VerCrd[k] = float4(c[0], c[1], c[2], c[3]);
+      }
+      for(int k=0;k<6;k++)
+      {
+         const float *c = &mid[ 4 * (size_t)tedg[ 6*(size_t)cnt + k ] ];
+         MidCrd[k] = float4(c[0], c[1], c[2], c[3]);
+      }
+      {
+#include "P2Quality/quality.cl"
+      }
+      out[cnt] = qal;
    }
 }
 

@@ -9,7 +9,11 @@ coordinates, residuals) plus the ball tables built by the reference's chained
 hash algorithm (oracle.c).  Tests then pin the oracle and the GPU path to
 these values on machines without the reference tree.
 
-Usage:  python tests/golden/make_golden.py
+p2_n5.npz holds a quadratic-tet mesh (gmlib_gb300.p2_mesh: vertices, unique
+edges with curved mid-edge nodes, the tet -> edge table) and the quality of
+the reference's examples/P2Quality/quality.cl body on it.
+
+Usage:  python tests/golden/make_golden.py [p2]     (p2: that fixture only)
 """
 import os
 import sys
@@ -39,8 +43,18 @@ def make(name, n, split, jitter, seed):
     print(name, len(crd), len(tet), "maxdeg", deg.max(), "maxpos", mp, "high", hs)
 
 
+def make_p2(name, n, split, jitter, curve, seed):
+    crd, tet, edges, mid, tedg = G.p2_mesh(n, split=split, jitter=jitter, curve=curve, seed=seed)
+    q = O.ref_p2_quality(crd, mid, tet, tedg)
+    np.savez_compressed(os.path.join(OUT, name), crd=crd, tet=tet, edges=edges, mid=mid,
+                        tedg=tedg, quality=q)
+    print(name, len(crd), len(tet), len(edges), "quality min %.6g mean %.6g" % (q.min(), q.mean()))
+
+
 if __name__ == "__main__":
     if O.refcl() is None:
         sys.exit("the reference tree is needed to generate the golden fixtures")
-    make("kuhn_n5.npz", 5, 0, 0.25, 12345)
-    make("reflected_n6.npz", 6, 1, 0.3, 777)
+    if sys.argv[1:] != ["p2"]:
+        make("kuhn_n5.npz", 5, 0, 0.25, 12345)
+        make("reflected_n6.npz", 6, 1, 0.3, 777)
+    make_p2("p2_n5.npz", 5, 1, 0.15, 0.08, 4242)

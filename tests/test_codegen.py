@@ -151,12 +151,43 @@ def test_dialect_rewrites(G):
     del rw
 
 
+def p2_data(G, g, v, tet):
+    """Edges, mid-edge nodes on the edges (MidCrd) and the tet quality (qal),
+    as the reference's P2Quality example declares them; the tetrahedron ->
+    edge downlink is built when the kernel is compiled."""
+    loc = np.array(G.TET_EDGES)
+    pairs = np.sort(np.stack([tet[:, loc[:, 0]], tet[:, loc[:, 1]]], axis=2), axis=2).reshape(-1, 2)
+    edges = np.unique(pairs, axis=0).astype(np.int32)
+    e = G.lib.GmlNewMeshData(g, G.GmlEdges, len(edges))
+    assert e and G.lib.GmlxSetData(g, e, G.as_ptr(edges), edges.nbytes)
+    m = G.lib.GmlNewSolutionData(g, G.GmlEdges, 1, G.GmlFlt4, b"MidCrd")
+    q = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 1, G.GmlFlt, b"qal")
+    return [(v, G.GmlReadMode, 0), (m, G.GmlReadMode, 0), (q, G.GmlWriteMode, 0)]
+
+
+def test_p2_downlink_naming_contract(G, offline):
+    """A tetrahedron kernel reading edge data gathers it through the
+    tetrahedron -> edge downlink (default name <Src><Dst>Lnk, an int8 line
+    per tet: 6 edges in the local edge order, then zero padding) into a local
+    array as wide as the link line."""
+    g = offline
+    crd, tet, v, t = mesh(G, g)
+    dats = p2_data(G, g, v, tet)
+    k = G.compile_kernel(g, G.p2_body(), "p2quality", G.GmlTetrahedra, dats)
+    assert k
+    s = source(G, g, k)
+    assert "const int8 *__restrict__ TetEdgLnkTab" in s and "float4 MidCrd[8];" in s
+    for j in range(6):
+        assert "MidCrd[%d] =  MidCrdTab[ TetEdgLnk.s%d ]" % (j, j) in s
+
+
 @pytest.mark.parametrize("kernel,msh,spec", [
     ("MeshQuality/compute_quality.cl", "tet", "quality"),
     ("NodeSmoothing/scatter.cl", "tet", "scatter"),
     ("NodeSmoothing/gather.cl", "ver", "gather"),
     ("GpuBandwidth/vertices_ball.cl", "ver", "ball"),
     ("TestFeatures/uplink.cl", "ver", "uplink"),
+    ("P2Quality/quality.cl", "tet", "p2"),
 ])
 def test_reference_example_bodies_compile_unchanged(G, offline, kernel, msh, spec):
     """The reference's own example bodies, read from its tree, compile
@@ -183,6 +214,8 @@ def test_reference_example_bodies_compile_unchanged(G, offline, kernel, msh, spe
         vd = G.lib.GmlNewSolutionData(g, G.GmlVertices, 1, G.GmlFlt4, b"VerDat")
         td = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 1, G.GmlFlt4, b"TetDat")
         dats = [(vd, G.GmlWriteMode, 0), (td, G.GmlReadMode, 0)]
+    elif spec == "p2":
+        dats = p2_data(G, g, v, tet)
     else:
         s = G.lib.GmlNewSolutionData(g, G.GmlVertices, 2, G.GmlFlt4, b"SolAtVer")
         m = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 1, G.GmlFlt4, b"TetMid")

@@ -1,6 +1,7 @@
-"""Generated kernels on the GPU against the oracle: the MeshQuality and
-NodeSmoothing flows of the reference (downlink gather, ball gather with
-voyeurs, high-degree twin kernels), reductions, argmin, ball tables."""
+"""Generated kernels on the GPU against the oracle: the MeshQuality,
+NodeSmoothing and P2Quality flows of the reference (downlink gathers, ball
+gather with voyeurs, high-degree twin kernels), reductions, argmin, ball
+tables."""
 import ctypes
 import os
 import subprocess
@@ -52,6 +53,43 @@ def test_quality_matches_golden(G, gpu, case):
     v, t = setup_mesh(G, gpu, gd["crd"], gd["tet"], gd["ref"])
     q, qg = quality_gpu(G, gpu, v, len(gd["tet"]))
     assert np.max(np.abs(qg - gd["quality"])) <= 2e-5 * np.max(np.abs(gd["quality"]))
+
+
+def p2_quality_gpu(G, g, crd, tet, edges, mid):
+    """The P2Quality flow: tets read vertex coordinates through TetVer and
+    mid-edge nodes through the tetrahedron -> edge downlink."""
+    G.lib.GmlNewParameters(g, 8, PARAMS)
+    v, t, e, m = G.upload_p2(g, crd, tet, edges, mid)
+    q = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 1, G.GmlFlt, b"qal")
+    k = G.compile_kernel(g, G.p2_body(), "p2quality", G.GmlTetrahedra,
+                         [(v, G.GmlReadMode, 0), (m, G.GmlReadMode, 0), (q, G.GmlWriteMode, 0)])
+    assert k
+    assert G.lib.GmlLaunchKernel(g, k) == 1
+    return q, G.get_data(g, q, np.float32, len(tet))
+
+
+# FP32 kernel against the FP64 oracle: triple products of control-net vectors
+# and square roots in FP32, fast_length / fast_distance
+P2_ATOL, P2_RTOL = 2e-5, 2e-4
+
+
+@pytest.mark.parametrize("n,split,curve", [(12, 0, 0.1), (9, 1, 0.2)])
+def test_p2_quality_matches_oracle(G, O, gpu, n, split, curve):
+    crd, tet, edges, mid, tedg = G.p2_mesh(n, split=split, jitter=0.2, curve=curve, seed=n)
+    q, qg = p2_quality_gpu(G, gpu, crd, tet, edges, mid)
+    qo = O.p2_quality(crd, mid, tet, tedg)
+    assert np.all(np.abs(qg - qo) <= P2_ATOL + P2_RTOL * np.abs(qo))
+    # the example's own reductions: mean and minimum of the tet qualities
+    assert G.reduce(gpu, q, G.GmlSum) == pytest.approx(float(np.sum(qg, dtype=np.float64)),
+                                                       rel=1e-12, abs=1e-12)
+    assert G.reduce(gpu, q, G.GmlMin) == float(qg.min())
+
+
+def test_p2_quality_matches_golden(G, gpu):
+    """Against the reference's P2Quality body evaluated on the CPU."""
+    gd = dict(np.load(os.path.join(GOLD, "p2_n5.npz")))
+    q, qg = p2_quality_gpu(G, gpu, gd["crd"], gd["tet"], gd["edges"], gd["mid"])
+    assert np.all(np.abs(qg - gd["quality"]) <= P2_ATOL + P2_RTOL * np.abs(gd["quality"]))
 
 
 def test_reductions_match_oracle(G, O, gpu):

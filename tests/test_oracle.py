@@ -107,3 +107,55 @@ def test_refcl_fresh_mesh(O, G):
     q = O.quality_ref(crd, tet)
     qr = O.ref_quality(crd, tet)
     assert np.max(np.abs(q - qr)) <= 1e-6 * np.max(np.abs(q))
+
+
+# P2 quality: FP64 restatement against the reference body evaluated in FP32;
+# the tolerance covers the FP32 rounding of the triple products and roots
+P2_ATOL, P2_RTOL = 2e-6, 1e-4
+
+
+def test_p2_quality_matches_reference_body(O):
+    g = load("p2_n5.npz")
+    q = O.p2_quality(g["crd"], g["mid"], g["tet"], g["tedg"])
+    assert np.all(np.abs(q - g["quality"]) <= P2_ATOL + P2_RTOL * np.abs(q))
+    assert (q < 0).any() and (q > 0.5).any()     # the fixture has inverted and good elements
+
+
+def test_p2_quality_known_answers(O):
+    """Straight P2 tets (mid-edge nodes at the midpoints): the Jacobian is
+    constant and V2 = V1, so q is the shape factor 2 sqrt(6) V / (L S) with
+    V = 6 vol, S = 2 area sum; 1 for the regular tetrahedron; curving an edge
+    outward lowers it."""
+    s = np.sqrt(2.0)
+    crd = np.array([[1, 0, -1 / s, 0], [-1, 0, -1 / s, 0], [0, 1, 1 / s, 0], [0, -1, 1 / s, 0]],
+                   np.float32)
+    tet = np.array([[0, 1, 2, 3]], np.int32)
+    if np.linalg.det(crd[1:, :3] - crd[0, :3]) < 0:
+        tet = tet[:, [0, 2, 1, 3]]
+    loc = [(0, 1), (1, 2), (2, 0), (3, 0), (3, 1), (3, 2)]
+    mid = np.zeros((6, 4), np.float32)
+    for e, (a, b) in enumerate(loc):
+        mid[e, :3] = 0.5 * (crd[tet[0, a], :3] + crd[tet[0, b], :3])
+    tedg = np.arange(6, dtype=np.int32)[None, :]
+    q = O.p2_quality(crd, mid, tet, tedg)
+    assert q[0] == pytest.approx(1.0, abs=1e-6)
+    # a right-angle corner tet: shape factor by hand
+    crd2 = np.array([[0, 0, 0, 0], [1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0]], np.float32)
+    mid2 = np.zeros((6, 4), np.float32)
+    for e, (a, b) in enumerate(loc):
+        mid2[e, :3] = 0.5 * (crd2[a, :3] + crd2[b, :3])
+    q2 = O.p2_quality(crd2, mid2, np.array([[0, 1, 2, 3]], np.int32), tedg)
+    area = 3 * 0.5 + np.sqrt(3) / 2
+    assert q2[0] == pytest.approx(2 * np.sqrt(6) * 1.0 / (np.sqrt(2) * 2 * area), rel=1e-12)
+    mid2[1, :3] += 0.05                          # edge (1,2) bent outward
+    q3 = O.p2_quality(crd2, mid2, np.array([[0, 1, 2, 3]], np.int32), tedg)
+    assert 0 < q3[0] < q2[0]
+
+
+def test_p2_refcl_fresh_mesh(O, G):
+    if O.refcl() is None:
+        pytest.skip("reference tree not present")
+    crd, tet, edges, mid, tedg = G.p2_mesh(6, split=0, jitter=0.25, curve=0.1, seed=5)
+    q = O.p2_quality(crd, mid, tet, tedg)
+    qr = O.ref_p2_quality(crd, mid, tet, tedg)
+    assert np.all(np.abs(q - qr) <= P2_ATOL + P2_RTOL * np.abs(q))
