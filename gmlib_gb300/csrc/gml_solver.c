@@ -14,6 +14,13 @@
  *      r = b - A x with the FP64 matrix, |r|        (FP64)
  *   until |r| <= tol |b|
  *
+ * An FP64 iteration is three kernels: q = A p with per-block partials of
+ * p.q; the update (folds the partials into alpha, x, r and |r|^2, sets beta
+ * and the stop flag); p = r + beta p.  An FP32 iteration is two: the SpMV
+ * forms p = r + beta p_old line by line from r and the previous direction
+ * (double-buffered by iteration parity) and writes it, then the update.  On
+ * this part the FP64 pipe makes that fused form slower in FP64.
+ *
  * Both stop on the relative residual.  Iterations run as CUDA graphs of
  * GML_CG_CHUNK iterations replayed on the instance's stream; the scalars stay
  * on the device, and the host reads them once per replay while the next
@@ -34,17 +41,18 @@
 #include "gml_mesh.h"
 #include "gml_solver.h"
 
-#define GML_CG_CHUNK  8          /* iterations per graph replay */
+#define GML_CG_CHUNK  8          /* iterations per graph replay (even: parity of p) */
 #define GML_CG_MAXOUT 20         /* refinement steps */
 
 typedef struct
 {
+   GmlMatSct   *mat;             /* the FP64 matrix solved with */
    int         nrow, B, vs;
    size_t      n;                /* scalars of a vector: rows x lanes */
    GmlSellDev  A32;              /* FP32 values, structure shared with the FP64 matrix */
    int         have32;
-   double      *b64, *x64, *r64, *p64, *q64, *part;
-   float       *d32, *r32, *p32, *q32;
+   double      *b64, *x64, *r64, *p64, *q64, *part, *spart;
+   float       *d32, *r32, *p32[2], *q32;     /* p32[0], p32[1]: directions by parity */
    GmdSvScal   *sc, *hsc;        /* device scalars, pinned host copies (2 slots) */
    void        *g64, *g32;       /* graphs of GML_CG_CHUNK iterations */
    void        *ev[2], *t0, *t1;
@@ -59,12 +67,14 @@ static double inner_factor(void)
    return f > 0. && f < 1. ? f : 1e-5;
 }
 
-/* iterations per graph replay (GML_CG_CHUNK overrides, 1..64) */
+/* iterations per graph replay (GML_CG_CHUNK overrides, 2..64, rounded up
+   to even so that every replay starts on direction buffer 0) */
 static int cg_chunk(void)
 {
    const char *e = getenv("GML_CG_CHUNK");
    int c = e ? atoi(e) : 0;
-   return c >= 1 && c <= 64 ? c : GML_CG_CHUNK;
+   c = c >= 1 && c <= 64 ? c : GML_CG_CHUNK;
+   return (c + 1) & ~1;
 }
 
 static void solver_free(GmlSct *gml, GmlSolver *s)
@@ -73,8 +83,8 @@ static void solver_free(GmlSct *gml, GmlSolver *s)
       return;
    gmd_free(gml->dev, s->b64); gmd_free(gml->dev, s->x64); gmd_free(gml->dev, s->r64);
    gmd_free(gml->dev, s->p64); gmd_free(gml->dev, s->q64); gmd_free(gml->dev, s->part);
-   gmd_free(gml->dev, s->d32); gmd_free(gml->dev, s->r32); gmd_free(gml->dev, s->p32);
-   gmd_free(gml->dev, s->q32); gmd_free(gml->dev, s->sc);
+   gmd_free(gml->dev, s->d32); gmd_free(gml->dev, s->r32); gmd_free(gml->dev, s->p32[0]);
+   gmd_free(gml->dev, s->p32[1]); gmd_free(gml->dev, s->q32); gmd_free(gml->dev, s->sc);
    if(s->have32)
       gmd_free(gml->dev, s->A32.Val);
    gmd_host_free(s->hsc);
@@ -110,6 +120,7 @@ static GmlSolver *solver_get(GmlSct *gml, GmlMatSct *mat, int mixed)
       s = calloc(1, sizeof(GmlSolver));
       if(!s)
          return NULL;
+      s->mat = mat;
       s->nrow = A->NmbLin;
       s->B = A->BlkSiz;
       s->vs = gmd_sv_lanes(A->BlkSiz);
@@ -117,7 +128,8 @@ static GmlSolver *solver_get(GmlSct *gml, GmlMatSct *mat, int mixed)
       s->b64 = gmd_alloc(gml->dev, n * 8);
       s->x64 = gmd_alloc(gml->dev, n * 8);
       s->r64 = gmd_alloc(gml->dev, n * 8);
-      s->part = gmd_alloc(gml->dev, GMD_SV_MAXBLK * 8);
+      s->part = gmd_alloc(gml->dev, 2 * GMD_SV_MAXBLK * 8);
+      s->spart = s->part + GMD_SV_MAXBLK;     /* SpMV partials, read by the update */
       s->sc = gmd_alloc(gml->dev, sizeof(GmdSvScal));
       s->hsc = gmd_host_alloc(2 * sizeof(GmdSvScal));
       s->ev[0] = gmd_event_new_sync();
@@ -147,9 +159,10 @@ static GmlSolver *solver_get(GmlSct *gml, GmlMatSct *mat, int mixed)
       s->A32.Val = gmd_alloc(gml->dev, nv * 4);
       s->d32 = gmd_alloc(gml->dev, s->n * 4);
       s->r32 = gmd_alloc(gml->dev, s->n * 4);
-      s->p32 = gmd_alloc(gml->dev, s->n * 4);
+      s->p32[0] = gmd_alloc(gml->dev, s->n * 4);
+      s->p32[1] = gmd_alloc(gml->dev, s->n * 4);
       s->q32 = gmd_alloc(gml->dev, s->n * 4);
-      if(!s->A32.Val || !s->d32 || !s->r32 || !s->p32 || !s->q32)
+      if(!s->A32.Val || !s->d32 || !s->r32 || !s->p32[0] || !s->p32[1] || !s->q32)
          return NULL;
       if(!gmd_sv_to_f32(gml->dev, (const double *)A->Val, (float *)s->A32.Val, nv))
          return NULL;
@@ -159,17 +172,36 @@ static GmlSolver *solver_get(GmlSct *gml, GmlMatSct *mat, int mixed)
    return s;
 }
 
-/* one CG iteration on (x, r, p, q) of scalar size fs with matrix A */
-static int cg_iteration(GmlSct *gml, GmlSolver *s, const GmlSellDev *A, int fs,
-                        void *x, void *r, void *p, void *q)
+/* the kernels of CG iteration i: FP64 on (x64, r64, p64, q64), three
+   kernels; FP32 on (d32, r32, p32[i & 1] -> p32[~i & 1], q32), two.  Kernel k
+   of the iteration is launched between the calls mark(k) and mark(k + 1)
+   when mark is given (per-kernel timing). */
+static int cg_iteration(GmlSct *gml, GmlSolver *s, int fs, int i,
+                        int (*mark)(GmlSct *, GmlSolver *, int))
 {
-   return gmd_sv_spmv_dot(gml->dev, A, p, q, s->part, s->sc)
-       && gmd_sv_update(gml->dev, fs, s->n, x, r, p, q, s->part, s->sc)
-       && gmd_sv_dir(gml->dev, fs, s->n, p, r, s->sc);
+   const int nsp = gmd_sv_spmv_blocks(s->nrow);
+   GmlSellDev *A64 = (GmlSellDev *)s->mat->Val;
+   if(fs == 8)
+      return (!mark || mark(gml, s, 0))
+          && gmd_sv_spmv(gml->dev, A64, NULL, s->p64, NULL, s->q64, s->spart, s->sc)
+          && (!mark || mark(gml, s, 1))
+          && gmd_sv_update(gml->dev, 8, s->n, s->x64, s->r64, s->p64, s->q64, s->spart, nsp,
+                           s->part, s->sc)
+          && (!mark || mark(gml, s, 2))
+          && gmd_sv_dir(gml->dev, 8, s->n, s->p64, s->r64, s->sc)
+          && (!mark || mark(gml, s, 3));
+   {
+      float *po = s->p32[i & 1], *pn = s->p32[(i & 1) ^ 1];
+      return (!mark || mark(gml, s, 0))
+          && gmd_sv_spmv(gml->dev, &s->A32, s->r32, po, pn, s->q32, s->spart, s->sc)
+          && (!mark || mark(gml, s, 1))
+          && gmd_sv_update(gml->dev, 4, s->n, s->d32, s->r32, pn, s->q32, s->spart, nsp,
+                           s->part, s->sc)
+          && (!mark || mark(gml, s, 2));
+   }
 }
 
-static int capture(GmlSct *gml, GmlSolver *s, const GmlSellDev *A, int fs,
-                   void *x, void *r, void *p, void *q, void **graph)
+static int capture(GmlSct *gml, GmlSolver *s, int fs, void **graph)
 {
    int ok = 1;
    if(*graph)
@@ -177,7 +209,7 @@ static int capture(GmlSct *gml, GmlSolver *s, const GmlSellDev *A, int fs,
    if(!gmd_graph_begin(gml->dev))
       return 0;
    for(int i=0;i<s->chunk && ok;i++)
-      ok = cg_iteration(gml, s, A, fs, x, r, p, q);
+      ok = cg_iteration(gml, s, fs, i, NULL);
    if(!gmd_graph_end(gml->dev, graph))
       return 0;
    return ok;
@@ -237,33 +269,35 @@ static int trace_on(void)
    return on;
 }
 
+static int mark_event(GmlSct *gml, GmlSolver *s, int k)
+{
+   return gmd_event_record(gml->dev, s->tr[k]);
+}
+
 /* the iterations of run_cg, launched one by one with an event between the
    kernels; synchronises after each iteration */
-static int run_cg_timed(GmlSct *gml, GmlSolver *s, const GmlSellDev *A, int fs,
-                        void *x, void *r, void *p, void *q, int maxit)
+static int run_cg_timed(GmlSct *gml, GmlSolver *s, int fs, int maxit)
 {
+   const int nk = fs == 8 ? 3 : 2;
    double t[3] = {0., 0., 0.};
    int n = 0;
    GmdSvScal h;
    for(;;)
    {
-      if(!gmd_event_record(gml->dev, s->tr[0])
-      || !gmd_sv_spmv_dot(gml->dev, A, p, q, s->part, s->sc)
-      || !gmd_event_record(gml->dev, s->tr[1])
-      || !gmd_sv_update(gml->dev, fs, s->n, x, r, p, q, s->part, s->sc)
-      || !gmd_event_record(gml->dev, s->tr[2])
-      || !gmd_sv_dir(gml->dev, fs, s->n, p, r, s->sc)
-      || !gmd_event_record(gml->dev, s->tr[3])
-      || !read_scalars(gml, s, &h))
+      if(!cg_iteration(gml, s, fs, n, mark_event) || !read_scalars(gml, s, &h))
          return -1;
-      for(int k=0;k<3;k++)
+      for(int k=0;k<nk;k++)
          t[k] += gmd_event_elapsed_s(s->tr[k], s->tr[k+1]);
       n++;
       if(h.done || n > maxit)
          break;
    }
-   fprintf(stderr, "cg kernels fp%d: spmv_dot %.1f us  update %.1f us  dir %.1f us  (%d launches each)\n",
-           8 * fs, 1e6 * t[0] / n, 1e6 * t[1] / n, 1e6 * t[2] / n, n);
+   if(fs == 8)
+      fprintf(stderr, "cg kernels fp64: spmv %.1f us  update %.1f us  dir %.1f us  (%d launches each)\n",
+              1e6 * t[0] / n, 1e6 * t[1] / n, 1e6 * t[2] / n, n);
+   else
+      fprintf(stderr, "cg kernels fp32: spmv+dir %.1f us  update %.1f us  (%d launches each)\n",
+              1e6 * t[0] / n, 1e6 * t[1] / n, n);
    return h.done == 1 ? h.it : h.done == 2 ? -2 : -1;
 }
 
@@ -346,10 +380,9 @@ int GmlxSolveCG(size_t GmlIdx, int MatIdx, int RhsIdx, int SolIdx, int mode, dou
    {
       if(!gmd_sv_init(gml->dev, s->n, s->B, gml->dat[rv->idx].GpuMem, s->b64, s->x64, s->r64, s->p64,
                       8, s->part, s->sc, tol * tol, MaxIte)
-      || !capture(gml, s, A, 8, s->x64, s->r64, s->p64, s->q64, &s->g64))
+      || !capture(gml, s, 8, &s->g64))
          return -6;
-      r = trace_on() == 2 ? run_cg_timed(gml, s, A, 8, s->x64, s->r64, s->p64, s->q64, MaxIte)
-                          : run_cg(gml, s, s->g64, MaxIte);
+      r = trace_on() == 2 ? run_cg_timed(gml, s, 8, MaxIte) : run_cg(gml, s, s->g64, MaxIte);
       trace(gml, s, "fp64 cg", &tt, r);
       if(r < 0)
       {
@@ -366,19 +399,18 @@ int GmlxSolveCG(size_t GmlIdx, int MatIdx, int RhsIdx, int SolIdx, int mode, dou
       tin = inner_factor();
       if(!gmd_sv_init(gml->dev, s->n, s->B, gml->dat[rv->idx].GpuMem, s->b64, s->x64, s->r64, s->r64,
                       8, s->part, s->sc, tol * tol, MaxIte)
-      || !capture(gml, s, &s->A32, 4, s->d32, s->r32, s->p32, s->q32, &s->g32))
+      || !capture(gml, s, 4, &s->g32))
          return -6;
       if(!read_scalars(gml, s, &h))
          return -6;
       trace(gml, s, "init", &tt, 0);
       while(h.rt > tol * tol * h.bb && out < GML_CG_MAXOUT && it < MaxIte)
       {
-         if(!gmd_sv_ir_begin(gml->dev, s->n, s->r64, s->r32, s->p32, s->d32, s->part, s->sc,
+         if(!gmd_sv_ir_begin(gml->dev, s->n, s->r64, s->r32, s->p32[0], s->d32, s->part, s->sc,
                              tin * tin, MaxIte - it))
             return -6;
-         r = trace_on() == 2
-           ? run_cg_timed(gml, s, &s->A32, 4, s->d32, s->r32, s->p32, s->q32, MaxIte - it)
-           : run_cg(gml, s, s->g32, MaxIte - it);
+         r = trace_on() == 2 ? run_cg_timed(gml, s, 4, MaxIte - it)
+                             : run_cg(gml, s, s->g32, MaxIte - it);
          trace(gml, s, "fp32 cg", &tt, r);
          if(r < 0)
          {

@@ -5,9 +5,11 @@
  * All scalars of an iteration (residual norms, step lengths, stop test) live
  * in device memory in one GmdSvScal, so iterations run back to back on the
  * stream (and inside CUDA graphs) without host round trips; the host reads
- * the structure only to decide whether to replay more iterations.  Every
- * dot product is accumulated in FP64; the reductions are deterministic
- * (per-block partials folded in a fixed order by the last block).
+ * the structure only to decide whether to replay more iterations.  Dot
+ * products are accumulated per thread in the vectors' precision (FP32 as an
+ * error-free TwoSum pair) and combined in FP64 or float pairs; the
+ * reductions are deterministic (per-block partials folded in a fixed order,
+ * by the last block or by every block of the next kernel).
  */
 #ifndef GML_SOLVER_H
 #define GML_SOLVER_H
@@ -46,13 +48,19 @@ int  gmd_sv_init(struct GmdCtx *ctx, size_t n, int B, const double *bsrc, double
                  void *x, void *r, void *p, int fltsiz, double *part, GmdSvScal *sc, double tol2,
                  int maxit);
 
-/* q = A p, pq = p.q, alpha = rr / pq */
-int  gmd_sv_spmv_dot(struct GmdCtx *ctx, const GmlSellDev *A, const void *p, void *q,
-                     double *part, GmdSvScal *sc);
+/* q = A p with the per-block partials of p.q in spart (gmd_sv_spmv_blocks
+   entries: float pairs for an FP32 matrix, doubles for FP64).  With r and
+   pn given, p is the previous direction and the product uses the new one,
+   r + beta p formed line by line and written to pn (pn != p). */
+int  gmd_sv_spmv(struct GmdCtx *ctx, const GmlSellDev *A, const void *r, const void *p,
+                 void *pn, void *q, void *spart, const GmdSvScal *sc);
+int  gmd_sv_spmv_blocks(int nrow);
 
-/* x += alpha p, r -= alpha q, rr' = |r|^2, beta = rr' / rr, stop test */
+/* pq = fold of the nsp SpMV partials, alpha = rr / pq, x += alpha p,
+   r -= alpha q, rr' = |r|^2, beta = rr' / rr, stop test (breakdown flag
+   when pq <= 0) */
 int  gmd_sv_update(struct GmdCtx *ctx, int fltsiz, size_t n, void *x, void *r, const void *p,
-                   const void *q, double *part, GmdSvScal *sc);
+                   const void *q, const void *spart, int nsp, double *part, GmdSvScal *sc);
 
 /* p = r + beta p */
 int  gmd_sv_dir(struct GmdCtx *ctx, int fltsiz, size_t n, void *p, const void *r,

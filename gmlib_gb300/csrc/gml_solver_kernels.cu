@@ -167,6 +167,7 @@ sv_init_kernel(size_t n, int B, int VS, const double *__restrict__ bsrc,
       sc->bb = tot;
       sc->rr = tot;
       sc->rt = tot;
+      sc->beta = 0.;
       sc->stop = tol2 * tot;
       sc->it = 0;
       sc->maxit = maxit;
@@ -174,16 +175,58 @@ sv_init_kernel(size_t n, int B, int VS, const double *__restrict__ bsrc,
    }
 }
 
-/* y = A x for the block row r (one thread per row); x lines of VS scalars */
-template<int B, int VS, class T>
+/* line c of a vector, VS scalars gathered with 16-byte loads */
+template<int VS, class T>
+__device__ __forceinline__ void sv_load_line(const T *__restrict__ v, size_t c, T out[VS])
+{
+   typedef typename Vec16<T>::type V;
+   const V *vp = reinterpret_cast<const V *>(v + c * VS);
+#pragma unroll
+   for(int u=0;u<VS/Vec16<T>::n;u++)
+   {
+      const V t = __ldg(vp + u);
+#pragma unroll
+      for(int i=0;i<Vec16<T>::n;i++)
+         out[ u * Vec16<T>::n + i ] = lane<T>(t, i);
+   }
+}
+
+/* the x lines of a product: a plain vector, or the CG direction formed on the
+   fly, p = r + beta p_old, one FMA per scalar (the same expression wherever a
+   line is formed, so every thread sees the same p) */
+template<int VS, class T> struct SvPlain
+{
+   const T *__restrict__ x;
+   __device__ __forceinline__ void operator()(size_t c, T out[VS]) const
+   {
+      sv_load_line<VS, T>(x, c, out);
+   }
+};
+
+template<int VS, class T> struct SvDirection
+{
+   const T *__restrict__ r;
+   const T *__restrict__ p;
+   T beta;
+   __device__ __forceinline__ void operator()(size_t c, T out[VS]) const
+   {
+      T rl[VS], pl[VS];
+      sv_load_line<VS, T>(r, c, rl);
+      sv_load_line<VS, T>(p, c, pl);
+#pragma unroll
+      for(int i=0;i<VS;i++)
+         out[i] = fma(beta, pl[i], rl[i]);
+   }
+};
+
+/* y = A x for the block row r (one thread per row); F fetches x lines */
+template<int B, int VS, class T, class F>
 __device__ __forceinline__ void sv_row_product(int r, const int64_t *__restrict__ soff,
                                                const int *__restrict__ deg,
                                                const int *__restrict__ col,
                                                const T *__restrict__ val,
-                                               const T *__restrict__ x, T y[VS])
+                                               const F &fetch, T y[VS])
 {
-   typedef typename Vec16<T>::type V;
-   constexpr int NV = VS / Vec16<T>::n;
    const int lane_ = r & 31;
    const int64_t base = __ldg(&soff[ r >> 5 ]);
    const int d = __ldg(&deg[r]);
@@ -197,15 +240,7 @@ __device__ __forceinline__ void sv_row_product(int r, const int64_t *__restrict_
    {
       const int c = __ldg(cp + (size_t)k * 32);
       T xv[VS];
-      const V *xp = reinterpret_cast<const V *>(x + (size_t)c * VS);
-#pragma unroll
-      for(int u=0;u<NV;u++)
-      {
-         const V t = __ldg(xp + u);
-#pragma unroll
-         for(int i=0;i<Vec16<T>::n;i++)
-            xv[ u * Vec16<T>::n + i ] = lane<T>(t, i);
-      }
+      fetch((size_t)c, xv);
       const T *blk = vp + (size_t)k * (B * B * 32);
 #pragma unroll
       for(int i=0;i<B;i++)
@@ -215,52 +250,150 @@ __device__ __forceinline__ void sv_row_product(int r, const int64_t *__restrict_
    }
 }
 
-template<int B, int VS, class T>
+/* ------------------------------------------------------------------------- */
+/* per-block dot partials handed from the SpMV to the update kernel: a       */
+/* TwoSum pair for FP32, a double for FP64.  The update kernel folds them in  */
+/* every block (same order, same result everywhere), so the SpMV needs no     */
+/* grid-wide ticket: its blocks end without a fence or an atomic.             */
+/* ------------------------------------------------------------------------- */
+
+template<class T> struct SvPart;
+template<> struct SvPart<float>  { typedef float2 type; };
+template<> struct SvPart<double> { typedef double type; };
+
+/* sum of two unevaluated float pairs, renormalised (TwoSum of the leading
+   parts, trailing parts added to the error) */
+__device__ __forceinline__ float2 sv_pair_add(float2 a, float2 b)
+{
+   const float s = a.x + b.x, bp = s - a.x;
+   const float e = ((a.x - (s - bp)) + (b.x - bp)) + (a.y + b.y);
+   const float h = s + e;
+   return make_float2(h, e - (h - s));
+}
+
+__device__ __forceinline__ float2 sv_part_zero(float2) { return make_float2(0.f, 0.f); }
+__device__ __forceinline__ double sv_part_zero(double) { return 0.; }
+__device__ __forceinline__ float2 sv_part_add(float2 a, float2 b) { return sv_pair_add(a, b); }
+__device__ __forceinline__ double sv_part_add(double a, double b) { return a + b; }
+__device__ __forceinline__ float2 sv_part_of(const SvAcc<float> &a) { return make_float2(a.s, a.c); }
+__device__ __forceinline__ double sv_part_of(const SvAcc<double> &a) { return a.s; }
+__device__ __forceinline__ double sv_part_value(float2 a) { return (double)a.x + (double)a.y; }
+__device__ __forceinline__ double sv_part_value(double a) { return a; }
+__device__ __forceinline__ float2 sv_shfl_down(float2 v, int o)
+{
+   return make_float2(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o));
+}
+__device__ __forceinline__ double sv_shfl_down(double v, int o)
+{
+   return __shfl_down_sync(0xffffffffu, v, o);
+}
+
+/* block fold of one partial per thread, fixed tree; result in thread 0 */
+template<class P> __device__ __forceinline__ P sv_block_part(P v)
+{
+   __shared__ P sh[SV_THREADS / 32];
+   const int lane_ = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+   for(int o=16;o>0;o>>=1)
+      v = sv_part_add(v, sv_shfl_down(v, o));
+   __syncthreads();
+   if(lane_ == 0)
+      sh[wid] = v;
+   __syncthreads();
+   if(wid == 0)
+   {
+      v = lane_ < SV_THREADS / 32 ? sh[lane_] : sv_part_zero(v);
+#pragma unroll
+      for(int o=16;o>0;o>>=1)
+         v = sv_part_add(v, sv_shfl_down(v, o));
+   }
+   return v;
+}
+
+/* the value of np partials, folded in a fixed order, in every thread */
+template<class P> __device__ __forceinline__ double sv_fold_parts(const P *__restrict__ part, int np)
+{
+   __shared__ double val;
+   P a = sv_part_zero(P()), b = sv_part_zero(P());
+   int i = threadIdx.x;
+   for(;i+SV_THREADS<np;i+=2*SV_THREADS)
+   {
+      a = sv_part_add(a, __ldg(part + i));
+      b = sv_part_add(b, __ldg(part + i + SV_THREADS));
+   }
+   if(i < np)
+      a = sv_part_add(a, __ldg(part + i));
+   a = sv_block_part(sv_part_add(a, b));
+   if(threadIdx.x == 0)
+      val = sv_part_value(a);
+   __syncthreads();
+   return val;
+}
+
+/* q = A p for every row, with the block partials of p.q in spart.  FUSE:
+   p = r + beta p_old is formed on the fly from r and p_old and written to
+   pn (the CG direction update needs no pass of its own). */
+template<int B, int VS, class T, bool FUSE>
 __global__ void __launch_bounds__(SV_THREADS)
-sv_spmv_dot_kernel(int nrow, const int64_t *__restrict__ soff, const int *__restrict__ deg,
-                   const int *__restrict__ col, const T *__restrict__ val,
-                   const T *__restrict__ p, T *__restrict__ q, double *part, GmdSvScal *sc)
+sv_spmv_kernel(int nrow, const int64_t *__restrict__ soff, const int *__restrict__ deg,
+               const int *__restrict__ col, const T *__restrict__ val,
+               const T *__restrict__ r, const T *__restrict__ p, T *__restrict__ pn,
+               T *__restrict__ q, typename SvPart<T>::type *spart, const GmdSvScal *sc)
 {
    typedef typename Vec16<T>::type V;
    constexpr int NV = VS / Vec16<T>::n;
    SvAcc<T> acc;
-   double tot;
    if(sv_stopped(sc))
       return;
-   for(int r=blockIdx.x*blockDim.x+threadIdx.x;r<nrow;r+=gridDim.x*blockDim.x)
+   const T beta = FUSE ? (T)sc->beta : (T)0;
+   for(int row=blockIdx.x*blockDim.x+threadIdx.x;row<nrow;row+=gridDim.x*blockDim.x)
    {
-      T y[VS];
-      sv_row_product<B, VS, T>(r, soff, deg, col, val, p, y);
-      V *qp = reinterpret_cast<V *>(q + (size_t)r * VS);
-      const V *pp = reinterpret_cast<const V *>(p + (size_t)r * VS);
+      T y[VS], pr[VS];
+      if(FUSE)
+      {
+         const SvDirection<VS, T> f = {r, p, beta};
+         sv_row_product<B, VS, T>(row, soff, deg, col, val, f, y);
+         f((size_t)row, pr);
+      }
+      else
+      {
+         const SvPlain<VS, T> f = {p};
+         sv_row_product<B, VS, T>(row, soff, deg, col, val, f, y);
+         f((size_t)row, pr);
+      }
+      V *qp = reinterpret_cast<V *>(q + (size_t)row * VS);
+      V *pp = reinterpret_cast<V *>(pn + (size_t)row * VS);
 #pragma unroll
       for(int u=0;u<NV;u++)
       {
-         V t;
+         V t, w;
 #pragma unroll
          for(int i=0;i<Vec16<T>::n;i++)
+         {
             reinterpret_cast<T *>(&t)[i] = y[ u * Vec16<T>::n + i ];
+            reinterpret_cast<T *>(&w)[i] = pr[ u * Vec16<T>::n + i ];
+         }
          qp[u] = t;
-         acc.add(dot16<T>(__ldg(pp + u), t));
+         if(FUSE)
+            pp[u] = w;
+         acc.add(dot16<T>(w, t));
       }
    }
-   if(sv_grid_sum(acc.get(), part, sc, &tot))
    {
-      sc->pq = tot;
-      if(tot > 0.)
-         sc->alpha = sc->rr / tot;
-      else
-      {
-         sc->alpha = 0.;
-         sc->done = 2;
-      }
+      const typename SvPart<T>::type v = sv_block_part(sv_part_of(acc));
+      if(threadIdx.x == 0)
+         spart[ blockIdx.x ] = v;
    }
 }
 
+/* pq = the folded SpMV partials, alpha = rr / pq, x += alpha p, r -= alpha
+   q and |r|^2; the last block sets beta, rr and the stop flag (or the
+   breakdown flag when pq <= 0, with x and r left unchanged) */
 template<class T>
 __global__ void __launch_bounds__(SV_THREADS)
 sv_update_kernel(size_t n, T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
-                 const T *__restrict__ q, double *part, GmdSvScal *sc)
+                 const T *__restrict__ q, const typename SvPart<T>::type *__restrict__ spart,
+                 int nsp, double *part, GmdSvScal *sc)
 {
    typedef typename Vec16<T>::type V;
    const size_t nv = n / Vec16<T>::n;
@@ -268,25 +401,35 @@ sv_update_kernel(size_t n, T *__restrict__ x, T *__restrict__ r, const T *__rest
    double tot;
    if(sv_stopped(sc))
       return;
-   const T a = (T)sc->alpha;
+   const double pq = sv_fold_parts(spart, nsp);
+   const double al = pq > 0. ? sc->rr / pq : 0.;
+   const T a = (T)al;
    V *xv = reinterpret_cast<V *>(x), *rv = reinterpret_cast<V *>(r);
    const V *pv = reinterpret_cast<const V *>(p), *qv = reinterpret_cast<const V *>(q);
-   for(size_t i=(size_t)blockIdx.x*blockDim.x+threadIdx.x;i<nv;i+=(size_t)gridDim.x*blockDim.x)
-   {
-      V xx = xv[i], rr = rv[i];
-      const V pp = pv[i], qq = qv[i];
-#pragma unroll
-      for(int k=0;k<Vec16<T>::n;k++)
+   if(pq > 0.)
+      for(size_t i=(size_t)blockIdx.x*blockDim.x+threadIdx.x;i<nv;i+=(size_t)gridDim.x*blockDim.x)
       {
-         reinterpret_cast<T *>(&xx)[k] += a * lane<T>(pp, k);
-         reinterpret_cast<T *>(&rr)[k] -= a * lane<T>(qq, k);
+         V xx = xv[i], rr = rv[i];
+         const V pp = pv[i], qq = qv[i];
+#pragma unroll
+         for(int k=0;k<Vec16<T>::n;k++)
+         {
+            reinterpret_cast<T *>(&xx)[k] += a * lane<T>(pp, k);
+            reinterpret_cast<T *>(&rr)[k] -= a * lane<T>(qq, k);
+         }
+         xv[i] = xx;
+         rv[i] = rr;
+         acc.add(dot16<T>(rr, rr));
       }
-      xv[i] = xx;
-      rv[i] = rr;
-      acc.add(dot16<T>(rr, rr));
-   }
    if(sv_grid_sum(acc.get(), part, sc, &tot))
    {
+      sc->pq = pq;
+      sc->alpha = al;
+      if(!(pq > 0.))
+      {
+         sc->done = 2;
+         return;
+      }
       sc->beta = tot / sc->rr;
       sc->rr = tot;
       sc->it += 1;
@@ -328,7 +471,8 @@ sv_residual_kernel(int nrow, const int64_t *__restrict__ soff, const int *__rest
    for(int r=blockIdx.x*blockDim.x+threadIdx.x;r<nrow;r+=gridDim.x*blockDim.x)
    {
       double y[VS];
-      sv_row_product<B, VS, double>(r, soff, deg, col, val, x, y);
+      const SvPlain<VS, double> f = {x};
+      sv_row_product<B, VS, double>(r, soff, deg, col, val, f, y);
 #pragma unroll
       for(int i=0;i<VS;i++)
       {
@@ -361,6 +505,7 @@ sv_ir_begin_kernel(size_t n, const double *__restrict__ r64, float *__restrict__
    if(sv_grid_sum(acc.get(), part, sc, &tot))
    {
       sc->rr = tot;
+      sc->beta = 0.;
       sc->stop = tin2 * tot;
       sc->it = 0;
       sc->maxit = maxit;
@@ -460,46 +605,64 @@ extern "C" int gmd_sv_init(GmdCtx *ctx, size_t n, int B, const double *bsrc, dou
 }
 
 template<int B, int VS, class T>
-static void sv_spmv_launch(cudaStream_t st, const GmlSellDev *A, const void *p, void *q,
-                           double *part, GmdSvScal *sc)
+static void sv_spmv_launch(cudaStream_t st, const GmlSellDev *A, const void *r, const void *p,
+                           void *pn, void *q, void *spart, const GmdSvScal *sc)
 {
-   sv_spmv_dot_kernel<B, VS, T><<<sv_row_grid(A->NmbLin), SV_THREADS, 0, st>>>(A->NmbLin,
-      A->SlcOff, A->Deg, A->Col, (const T *)A->Val, (const T *)p, (T *)q, part, sc);
+   typedef typename SvPart<T>::type P;
+   const unsigned g = sv_row_grid(A->NmbLin);
+   if(r)
+      sv_spmv_kernel<B, VS, T, true><<<g, SV_THREADS, 0, st>>>(A->NmbLin, A->SlcOff, A->Deg,
+         A->Col, (const T *)A->Val, (const T *)r, (const T *)p, (T *)pn, (T *)q, (P *)spart, sc);
+   else
+      sv_spmv_kernel<B, VS, T, false><<<g, SV_THREADS, 0, st>>>(A->NmbLin, A->SlcOff, A->Deg,
+         A->Col, (const T *)A->Val, NULL, (const T *)p, NULL, (T *)q, (P *)spart, sc);
 }
 
 template<class T>
-static int sv_spmv_t(cudaStream_t st, const GmlSellDev *A, const void *p, void *q,
-                     double *part, GmdSvScal *sc)
+static int sv_spmv_t(cudaStream_t st, const GmlSellDev *A, const void *r, const void *p,
+                     void *pn, void *q, void *spart, const GmdSvScal *sc)
 {
    switch(A->BlkSiz)
    {
-      case 3: sv_spmv_launch<3, 4, T>(st, A, p, q, part, sc); break;
-      case 4: sv_spmv_launch<4, 4, T>(st, A, p, q, part, sc); break;
-      case 5: sv_spmv_launch<5, 8, T>(st, A, p, q, part, sc); break;
-      case 7: sv_spmv_launch<7, 8, T>(st, A, p, q, part, sc); break;
+      case 3: sv_spmv_launch<3, 4, T>(st, A, r, p, pn, q, spart, sc); break;
+      case 4: sv_spmv_launch<4, 4, T>(st, A, r, p, pn, q, spart, sc); break;
+      case 5: sv_spmv_launch<5, 8, T>(st, A, r, p, pn, q, spart, sc); break;
+      case 7: sv_spmv_launch<7, 8, T>(st, A, r, p, pn, q, spart, sc); break;
       default: return 0;
    }
    return sv_ok();
 }
 
-extern "C" int gmd_sv_spmv_dot(GmdCtx *ctx, const GmlSellDev *A, const void *p, void *q,
-                               double *part, GmdSvScal *sc)
+extern "C" int gmd_sv_spmv_blocks(int nrow)
+{
+   return (int)sv_row_grid(nrow);
+}
+
+extern "C" int gmd_sv_spmv(GmdCtx *ctx, const GmlSellDev *A, const void *r, const void *p,
+                           void *pn, void *q, void *spart, const GmdSvScal *sc)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
-   return A->FltSiz == 8 ? sv_spmv_t<double>(st, A, p, q, part, sc)
-                         : sv_spmv_t<float>(st, A, p, q, part, sc);
+   if((r == NULL) != (pn == NULL))
+      return 0;
+   return A->FltSiz == 8 ? sv_spmv_t<double>(st, A, r, p, pn, q, spart, sc)
+                         : sv_spmv_t<float>(st, A, r, p, pn, q, spart, sc);
 }
 
 extern "C" int gmd_sv_update(GmdCtx *ctx, int fltsiz, size_t n, void *x, void *r,
-                             const void *p, const void *q, double *part, GmdSvScal *sc)
+                             const void *p, const void *q, const void *spart, int nsp,
+                             double *part, GmdSvScal *sc)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   if(nsp < 1 || nsp > GMD_SV_MAXBLK)
+      return 0;
    if(fltsiz == 8)
-      sv_update_kernel<double><<<sv_flat_grid(ctx, n / 2, sv_update_occ<double>()), SV_THREADS, 0, st>>>(n, (double *)x,
-         (double *)r, (const double *)p, (const double *)q, part, sc);
+      sv_update_kernel<double><<<sv_flat_grid(ctx, n / 2, sv_update_occ<double>()), SV_THREADS,
+         0, st>>>(n, (double *)x, (double *)r, (const double *)p, (const double *)q,
+                  (const double *)spart, nsp, part, sc);
    else
-      sv_update_kernel<float><<<sv_flat_grid(ctx, n / 4, sv_update_occ<float>()), SV_THREADS, 0, st>>>(n, (float *)x,
-         (float *)r, (const float *)p, (const float *)q, part, sc);
+      sv_update_kernel<float><<<sv_flat_grid(ctx, n / 4, sv_update_occ<float>()), SV_THREADS,
+         0, st>>>(n, (float *)x, (float *)r, (const float *)p, (const float *)q,
+                  (const float2 *)spart, nsp, part, sc);
    return sv_ok();
 }
 
