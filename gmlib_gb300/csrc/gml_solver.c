@@ -14,12 +14,13 @@
  *      r = b - A x with the FP64 matrix, |r|        (FP64)
  *   until |r| <= tol |b|
  *
- * An FP64 iteration is three kernels: q = A p with per-block partials of
- * p.q; the update (folds the partials into alpha, x, r and |r|^2, sets beta
- * and the stop flag); p = r + beta p.  An FP32 iteration is two: the SpMV
- * forms p = r + beta p_old line by line from r and the previous direction
- * (double-buffered by iteration parity) and writes it, then the update.  On
- * this part the FP64 pipe makes that fused form slower in FP64.
+ * An FP64 iteration is three kernels: q = A p and p.q (folded by its last
+ * block); the update (alpha, x, r and |r|^2, beta and the stop flag);
+ * p = r + beta p.  An FP32 iteration is two: the SpMV forms p = r + beta
+ * p_old line by line from r and the previous direction (double-buffered by
+ * iteration parity), writes it and leaves per-block partials of p.q, which
+ * every block of the update folds itself.  On this part the FP64 pipe makes
+ * the fused form slower in FP64.
  *
  * Both stop on the relative residual.  Iterations run as CUDA graphs of
  * GML_CG_CHUNK iterations replayed on the instance's stream; the scalars stay
@@ -185,7 +186,7 @@ static int cg_iteration(GmlSct *gml, GmlSolver *s, int fs, int i,
       return (!mark || mark(gml, s, 0))
           && gmd_sv_spmv(gml->dev, A64, NULL, s->p64, NULL, s->q64, s->spart, s->sc)
           && (!mark || mark(gml, s, 1))
-          && gmd_sv_update(gml->dev, 8, s->n, s->x64, s->r64, s->p64, s->q64, s->spart, nsp,
+          && gmd_sv_update(gml->dev, 8, s->n, s->x64, s->r64, s->p64, s->q64, s->spart, 0,
                            s->part, s->sc)
           && (!mark || mark(gml, s, 2))
           && gmd_sv_dir(gml->dev, 8, s->n, s->p64, s->r64, s->sc)

@@ -48,15 +48,16 @@ int  gmd_sv_init(struct GmdCtx *ctx, size_t n, int B, const double *bsrc, double
                  void *x, void *r, void *p, int fltsiz, double *part, GmdSvScal *sc, double tol2,
                  int maxit);
 
-/* q = A p with the per-block partials of p.q in spart (gmd_sv_spmv_blocks
-   entries: float pairs for an FP32 matrix, doubles for FP64).  With r and
-   pn given, p is the previous direction and the product uses the new one,
-   r + beta p formed line by line and written to pn (pn != p). */
+/* q = A p.  FP32 matrix: the per-block partials of p.q in spart
+   (gmd_sv_spmv_blocks float pairs); FP64: p.q in sc->pq (spart is the
+   scratch of that fold).  With r and pn given, p is the previous direction
+   and the product uses the new one, r + beta p formed line by line and
+   written to pn (pn != p). */
 int  gmd_sv_spmv(struct GmdCtx *ctx, const GmlSellDev *A, const void *r, const void *p,
-                 void *pn, void *q, void *spart, const GmdSvScal *sc);
+                 void *pn, void *q, void *spart, GmdSvScal *sc);
 int  gmd_sv_spmv_blocks(int nrow);
 
-/* pq = fold of the nsp SpMV partials, alpha = rr / pq, x += alpha p,
+/* pq = fold of the nsp SpMV partials (sc->pq when nsp = 0), alpha = rr / pq, x += alpha p,
    r -= alpha q, rr' = |r|^2, beta = rr' / rr, stop test (breakdown flag
    when pq <= 0) */
 int  gmd_sv_update(struct GmdCtx *ctx, int fltsiz, size_t n, void *x, void *r, const void *p,

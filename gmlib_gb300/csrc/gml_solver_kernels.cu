@@ -330,7 +330,8 @@ template<class P> __device__ __forceinline__ double sv_fold_parts(const P *__res
    return val;
 }
 
-/* q = A p for every row, with the block partials of p.q in spart.  FUSE:
+/* q = A p for every row.  FP32: the block partials of p.q in spart; FP64:
+   p.q folded by the last block into sc->pq.  FUSE:
    p = r + beta p_old is formed on the fly from r and p_old and written to
    pn (the CG direction update needs no pass of its own). */
 template<int B, int VS, class T, bool FUSE>
@@ -338,7 +339,7 @@ __global__ void __launch_bounds__(SV_THREADS)
 sv_spmv_kernel(int nrow, const int64_t *__restrict__ soff, const int *__restrict__ deg,
                const int *__restrict__ col, const T *__restrict__ val,
                const T *__restrict__ r, const T *__restrict__ p, T *__restrict__ pn,
-               T *__restrict__ q, typename SvPart<T>::type *spart, const GmdSvScal *sc)
+               T *__restrict__ q, typename SvPart<T>::type *spart, GmdSvScal *sc)
 {
    typedef typename Vec16<T>::type V;
    constexpr int NV = VS / Vec16<T>::n;
@@ -379,6 +380,16 @@ sv_spmv_kernel(int nrow, const int64_t *__restrict__ soff, const int *__restrict
          acc.add(dot16<T>(w, t));
       }
    }
+   if constexpr(sizeof(T) == 8)
+   {
+      /* FP64: this kernel is bound by the FP64 pipe, which hides a grid-wide
+         fold at its end, while a fold of every partial in each block of the
+         update kernel would cost that kernel ~25 %; pq goes to the scalars */
+      double tot;
+      if(sv_grid_sum(acc.get(), spart, sc, &tot))
+         sc->pq = tot;
+   }
+   else
    {
       const typename SvPart<T>::type v = sv_block_part(sv_part_of(acc));
       if(threadIdx.x == 0)
@@ -401,7 +412,7 @@ sv_update_kernel(size_t n, T *__restrict__ x, T *__restrict__ r, const T *__rest
    double tot;
    if(sv_stopped(sc))
       return;
-   const double pq = sv_fold_parts(spart, nsp);
+   const double pq = nsp ? sv_fold_parts(spart, nsp) : sc->pq;
    const double al = pq > 0. ? sc->rr / pq : 0.;
    const T a = (T)al;
    V *xv = reinterpret_cast<V *>(x), *rv = reinterpret_cast<V *>(r);
@@ -606,7 +617,7 @@ extern "C" int gmd_sv_init(GmdCtx *ctx, size_t n, int B, const double *bsrc, dou
 
 template<int B, int VS, class T>
 static void sv_spmv_launch(cudaStream_t st, const GmlSellDev *A, const void *r, const void *p,
-                           void *pn, void *q, void *spart, const GmdSvScal *sc)
+                           void *pn, void *q, void *spart, GmdSvScal *sc)
 {
    typedef typename SvPart<T>::type P;
    const unsigned g = sv_row_grid(A->NmbLin);
@@ -620,7 +631,7 @@ static void sv_spmv_launch(cudaStream_t st, const GmlSellDev *A, const void *r, 
 
 template<class T>
 static int sv_spmv_t(cudaStream_t st, const GmlSellDev *A, const void *r, const void *p,
-                     void *pn, void *q, void *spart, const GmdSvScal *sc)
+                     void *pn, void *q, void *spart, GmdSvScal *sc)
 {
    switch(A->BlkSiz)
    {
@@ -639,7 +650,7 @@ extern "C" int gmd_sv_spmv_blocks(int nrow)
 }
 
 extern "C" int gmd_sv_spmv(GmdCtx *ctx, const GmlSellDev *A, const void *r, const void *p,
-                           void *pn, void *q, void *spart, const GmdSvScal *sc)
+                           void *pn, void *q, void *spart, GmdSvScal *sc)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
    if((r == NULL) != (pn == NULL))
@@ -653,7 +664,7 @@ extern "C" int gmd_sv_update(GmdCtx *ctx, int fltsiz, size_t n, void *x, void *r
                              double *part, GmdSvScal *sc)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
-   if(nsp < 1 || nsp > GMD_SV_MAXBLK)
+   if(nsp < 0 || nsp > GMD_SV_MAXBLK)
       return 0;
    if(fltsiz == 8)
       sv_update_kernel<double><<<sv_flat_grid(ctx, n / 2, sv_update_occ<double>()), SV_THREADS,
