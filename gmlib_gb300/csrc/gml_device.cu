@@ -10,6 +10,7 @@
  * loads on hosts without a GPU driver.
  */
 #include <cuda_runtime.h>
+#include <stdint.h>
 #include <cuda.h>
 #include <nvrtc.h>
 #include <stdio.h>
@@ -28,6 +29,7 @@ struct GmdCtx
    cudaStream_t   stream;
    cudaStream_t   side;          /* second stream for concurrent graph branches */
    int            use_side;      /* 1: gmd_stream returns the side stream */
+   int            pageable;      /* kernels can address pageable host memory */
    char           err[512];
 };
 
@@ -129,6 +131,17 @@ extern "C" GmdCtx *gmd_init(int dev, int *fp64, char *err, int errlen)
    ctx->dev = dev;
    cudaGetDeviceProperties(&p, dev);
    ctx->nsm = p.multiProcessorCount;
+   {
+      /* GML_DIRECT=0 keeps whole-datatype transfers on the staged path */
+      const char *e = getenv("GML_DIRECT");
+      int v = 0;
+      if(cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess)
+      {
+         cudaGetLastError();
+         v = 0;
+      }
+      ctx->pageable = v && !(e && *e == '0');
+   }
 
    if(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
    {
@@ -200,6 +213,89 @@ extern "C" int gmd_stream_wait(GmdCtx *ctx, void *evt)
    return ok(ctx, cudaStreamWaitEvent((cudaStream_t)gmd_stream(ctx), (cudaEvent_t)evt, 0),
              "stream wait");
 }
+/* ------------------------------------------------------------------------- */
+/* direct whole-buffer transfers                                              */
+/* ------------------------------------------------------------------------- */
+
+/* 1 when kernels of the instance can read and write host memory at p:
+   any host memory where the device has pageable memory access (on this
+   platform, through the CPU's page tables over the chip-to-chip link), else
+   only pinned or registered memory mapped at the same address */
+extern "C" int gmd_host_addressable(GmdCtx *ctx, const void *p)
+{
+   cudaPointerAttributes a;
+   if(!ctx || !p)
+      return 0;
+   if(ctx->pageable)
+      return 1;
+   if(cudaPointerGetAttributes(&a, p) != cudaSuccess)
+   {
+      cudaGetLastError();
+      return 0;
+   }
+   return a.type == cudaMemoryTypeHost && a.devicePointer == p;
+}
+
+/* 1 when no work is pending on the instance's streams */
+extern "C" int gmd_idle(GmdCtx *ctx)
+{
+   cudaError_t r;
+   if(!ctx)
+      return 0;
+   r = cudaStreamQuery(ctx->stream);
+   if(r == cudaSuccess && ctx->side)
+      r = cudaStreamQuery(ctx->side);
+   if(r != cudaSuccess && r != cudaErrorNotReady)
+      return ok(ctx, r, "stream query");
+   return r == cudaSuccess;
+}
+
+/* n 16-byte words from src to d0 and, when d1 is given, to d1 as well: one
+   read of the source however many copies are written */
+__global__ void __launch_bounds__(256)
+fanout_kernel(const uint4 *__restrict__ src, uint4 *__restrict__ d0, uint4 *__restrict__ d1,
+              size_t n)
+{
+   const size_t st = (size_t)gridDim.x * blockDim.x;
+   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+   for(;i+3*st<n;i+=4*st)
+   {
+      const uint4 a = src[i], b = src[i + st], c = src[i + 2*st], d = src[i + 3*st];
+      d0[i] = a; d0[i + st] = b; d0[i + 2*st] = c; d0[i + 3*st] = d;
+      if(d1)
+      {
+         d1[i] = a; d1[i + st] = b; d1[i + 2*st] = c; d1[i + 3*st] = d;
+      }
+   }
+   for(;i<n;i+=st)
+   {
+      const uint4 a = src[i];
+      d0[i] = a;
+      if(d1)
+         d1[i] = a;
+   }
+}
+
+/* copy bytes from src to d0 (and d1 unless NULL) with one kernel on the
+   instance's stream; every pointer is device memory or host memory the
+   device can address (gmd_host_addressable), 16-byte aligned, and bytes a
+   multiple of 16.  Returns 0 (nothing launched) when those do not hold. */
+extern "C" int gmd_fanout(GmdCtx *ctx, const void *src, void *d0, void *d1, size_t bytes)
+{
+   size_t n = bytes / 16, g;
+   if(!ctx || !src || !d0 || (bytes & 15)
+   || (((uintptr_t)src | (uintptr_t)d0 | (uintptr_t)d1) & 15))
+      return 0;
+   if(!n)
+      return 1;
+   g = (n + 1023) / 1024;
+   if(g > (size_t)ctx->nsm * 8)
+      g = (size_t)ctx->nsm * 8;
+   fanout_kernel<<<(unsigned)g, 256, 0, ctx->stream>>>((const uint4 *)src, (uint4 *)d0,
+                                                      (uint4 *)d1, n);
+   return ok(ctx, cudaGetLastError(), "fan-out copy");
+}
+
 extern "C" const char *gmd_last_error(GmdCtx *ctx) { return ctx ? ctx->err : ""; }
 extern "C" int gmd_num_sms(GmdCtx *ctx) { return ctx ? ctx->nsm : 1; }
 

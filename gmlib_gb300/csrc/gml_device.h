@@ -45,6 +45,11 @@ int      gmd_d2h(GmdCtx *ctx, void *dst, const void *src, size_t bytes);
 int      gmd_d2h_async(GmdCtx *ctx, void *dst, const void *src, size_t bytes);
 int      gmd_d2d_async(GmdCtx *ctx, void *dst, const void *src, size_t bytes);
 int      gmd_memset_async(GmdCtx *ctx, void *dst, int val, size_t bytes);
+int      gmd_host_addressable(GmdCtx *ctx, const void *p);  /* kernels can use host pointer p */
+int      gmd_idle(GmdCtx *ctx);                               /* no work pending */
+/* one-kernel copy of bytes from src to d0 and d1 (d1 may be NULL); 0 when
+   the pointers are not 16-byte aligned or bytes is not a multiple of 16 */
+int      gmd_fanout(GmdCtx *ctx, const void *src, void *d0, void *d1, size_t bytes);
 
 /* events ------------------------------------------------------------------- */
 void    *gmd_event_new(void);

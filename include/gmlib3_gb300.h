@@ -86,9 +86,14 @@ int      GmlxCompileKernelV   (size_t, const char *src, const char *name, int Ms
                                const int *LnkTab);
 
 /* Whole-datatype copies between a caller buffer and a datatype, bytes equal
-   to the datatype size (lines x line size).  Set uploads (asynchronously),
-   Get downloads (blocking).  Bulk counterparts of GmlSetDataLine /
-   GmlGetDataLine (gmlib3.c:1841, 1910). */
+   to the datatype size (lines x line size).  Bulk counterparts of
+   GmlSetDataLine / GmlGetDataLine (gmlib3.c:1841, 1910): the host mirror
+   that the line accessors read holds the data set or downloaded.  Set has
+   consumed buf when it returns; it uploads asynchronously from the mirror,
+   or, for a large datatype on an idle instance whose device can address
+   buf (pinned memory, or pageable memory where the device has pageable
+   memory access), copies buf to the device and the mirror with one kernel
+   before returning.  Get is blocking. */
 int      GmlxSetData          (size_t, int DatIdx, const void *buf, size_t bytes);
 int      GmlxGetData          (size_t, int DatIdx, void *buf, size_t bytes);
 

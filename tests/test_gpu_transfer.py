@@ -1,0 +1,82 @@
+"""Whole-datatype transfers (GmlxSetData / GmlxGetData): the direct path
+(one kernel writing the destination and the host mirror) and the staged
+path (host copy into the mirror, DMA) give the same device data and the
+same mirror, which the line accessors read."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def instance(G, direct):
+    old = os.environ.get("GML_DIRECT")
+    os.environ["GML_DIRECT"] = "1" if direct else "0"
+    try:
+        g = G.lib.GmlInit(0)
+    finally:
+        if old is None:
+            del os.environ["GML_DIRECT"]
+        else:
+            os.environ["GML_DIRECT"] = old
+    assert g
+    return g
+
+
+def line(G, g, idx, lin):
+    """Vertex line lin through the reference accessor (reads the mirror for
+    lin > 0; line 0 downloads first)."""
+    x, y, z = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    ref = ctypes.c_int()
+    assert G.lib.GmlGetDataLine(ctypes.c_size_t(g), ctypes.c_int(idx), ctypes.c_int(lin),
+                                ctypes.byref(x), ctypes.byref(y), ctypes.byref(z),
+                                ctypes.byref(ref)) == 1
+    return x.value, y.value, z.value
+
+
+@pytest.mark.parametrize("direct", [True, False])
+@pytest.mark.parametrize("offset", [0, 4])
+def test_set_get_round_trip(G, direct, offset):
+    nv = 300_001                                   # 4.8 MB of float4 lines: above the direct threshold
+    rng = np.random.default_rng(7)
+    store = np.zeros(nv * 4 + 4, np.float32)       # offset 4 bytes: unaligned source, staged path
+    crd = store[offset // 4: offset // 4 + nv * 4].reshape(nv, 4)
+    crd[:, :3] = rng.uniform(-1, 1, (nv, 3))
+    g = instance(G, direct)
+    try:
+        v = G.lib.GmlNewMeshData(g, G.GmlVertices, nv)
+        assert v and G.lib.GmlxSetData(g, v, crd.ctypes.data, crd.nbytes) == 1
+        # the mirror holds what was set: line 7 is read from it without a
+        # download (line 0 downloads first)
+        assert line(G, g, v, 7) == tuple(float(c) for c in crd[7, :3])
+        assert line(G, g, v, 0) == tuple(float(c) for c in crd[0, :3])
+        out = np.zeros_like(crd)
+        assert G.lib.GmlxGetData(g, v, out.ctypes.data, out.nbytes) == 1
+        assert np.array_equal(out, crd)
+    finally:
+        G.lib.GmlStop(g)
+
+
+def test_get_refreshes_the_mirror(G):
+    """After a kernel changes the device data, GmlxGetData on either path
+    leaves the mirror equal to the downloaded data (as a download does)."""
+    n = 24
+    crd, tet, ref = G.cube_mesh(n, split=1, jitter=0.3, seed=3)
+    res = []
+    for direct in (True, False):
+        g = instance(G, direct)
+        try:
+            v, t = G.upload_mesh(g, crd, tet, ref)
+            assert G.lib.GmlxMeshSetup(g, 1) == 1
+            assert G.lib.GmlxSmooth(g, 3, ctypes.c_float(1.0)) == 1
+            out = np.zeros_like(crd)
+            assert G.lib.GmlxGetData(g, v, out.ctypes.data, out.nbytes) == 1
+            assert not np.array_equal(out, crd)          # the sweeps moved interior vertices
+            k = int(np.argmax(np.abs(out - crd).sum(axis=1)))
+            assert line(G, g, v, k) == tuple(float(c) for c in out[k, :3])
+            res.append(out)
+        finally:
+            G.lib.GmlStop(g)
+    assert np.array_equal(res[0], res[1])
