@@ -113,7 +113,7 @@ def solve(g, lin, col, val, rhs, mode, tol=1e-10, maxit=5000):
     ix = new_vector(g, np.zeros_like(rhs), G.GmlDbl)
     info = G.GmlxSolveInfo()
     rc = G.lib.GmlxSolveCG(g, m, ib, ix, mode, tol, maxit, ctypes.byref(info))
-    x = read_vector(g, ix, len(lin) - 1, 3, G.GmlDbl)
+    x = read_vector(g, ix, len(lin) - 1, val.shape[-1], G.GmlDbl)
     return rc, x, info
 
 
@@ -135,6 +135,48 @@ def test_cg_reaches_tolerance(O, gpu, mode, n, split):
         assert info.NmbOut == 1
     else:
         assert info.NmbOut >= 2
+
+
+def spd_blocks(lin, col, b, seed):
+    """An SPD system of b x b blocks on the (symmetric) sparsity of the cube
+    vertex graph: off-diagonal blocks uniform in [-1, 0] with A_ji = A_ij^T,
+    diagonal blocks diag(1 + sum of |entries| of the row), rhs in [-1, 1]."""
+    rng = np.random.default_rng(seed)
+    nrow = len(lin) - 1
+    row = np.repeat(np.arange(nrow), np.diff(lin))
+    key = row.astype(np.int64) * nrow + col
+    tkey = col.astype(np.int64) * nrow + row
+    order = np.argsort(key)
+    tpos = order[np.searchsorted(key[order], tkey)]          # index of block (j, i)
+    val = np.zeros((len(col), b, b))
+    upper = col > row
+    blk = rng.uniform(-1.0, 0.0, (int(upper.sum()), b, b))
+    val[upper] = blk
+    val[tpos[upper]] = np.transpose(blk, (0, 2, 1))
+    diag = col == row
+    absrow = np.zeros((nrow, b))
+    np.add.at(absrow, row[~diag], np.abs(val[~diag]).sum(axis=2))
+    val[diag] = np.eye(b)[None] * (1.0 + absrow[row[diag]])[:, :, None]
+    rhs = rng.uniform(-1.0, 1.0, (nrow, b))
+    return val, rhs
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [G.GmlxCgFp64, G.GmlxCgMixed])
+@pytest.mark.parametrize("b", [4, 5, 7])
+def test_cg_block_sizes(O, gpu, mode, b):
+    """The SpMV, update and fused direction kernels of every block size
+    (4- and 8-lane vector lines)."""
+    lin, col, _, _ = G.cube_spd(8, 1, seed=b)
+    val, rhs = spd_blocks(lin, col, b, seed=b)
+    rc, x, info = solve(gpu, lin, col, val, rhs, mode)
+    assert rc == 1, (rc, info.NmbIte, info.RelRes)
+    rel = O.rel_residual(lin, col, val, rhs, x)
+    assert rel <= 1e-10
+    xo, ito = O.cg(lin, col, val, rhs, 1e-10, 5000)
+    assert np.max(np.abs(x - xo)) <= 4e-10 * np.linalg.norm(rhs)
+    if mode == G.GmlxCgFp64:
+        assert abs(info.NmbIte - ito) <= 2
 
 
 @pytest.mark.gpu
