@@ -80,3 +80,26 @@ def test_get_refreshes_the_mirror(G):
         finally:
             G.lib.GmlStop(g)
     assert np.array_equal(res[0], res[1])
+
+
+def test_new_mirrors_start_zeroed(G):
+    """A datatype created after another instance used and freed the same
+    amount of pinned host memory still reads as zeros, as the reference's
+    calloc'd mirrors do."""
+    nv = 200_000                                   # 3.2 MB: a pinned mirror
+    crd = np.full((nv, 4), 7.0, np.float32)
+    g = instance(G, True)
+    g2 = instance(G, True)                         # a second instance stays alive meanwhile
+    try:
+        v = G.lib.GmlNewMeshData(g, G.GmlVertices, nv)
+        assert G.lib.GmlxSetData(g, v, crd.ctypes.data, crd.nbytes) == 1
+        G.lib.GmlStop(g)
+        g = instance(G, True)
+        v = G.lib.GmlNewMeshData(g, G.GmlVertices, nv)
+        assert line(G, g, v, 5) == (0.0, 0.0, 0.0)      # the mirror, not downloaded
+        out = np.ones_like(crd)
+        assert G.lib.GmlxGetData(g, v, out.ctypes.data, out.nbytes) == 1
+        assert not out.any()
+    finally:
+        G.lib.GmlStop(g)
+        G.lib.GmlStop(g2)
