@@ -68,9 +68,11 @@ typedef struct
    int            ntg, captg;
    /* run state */
    pthread_mutex_t mu;
-   pthread_cond_t cv_work, cv_done;
+   pthread_cond_t cv_work, cv_done, cv_reap;
    GmlxRequest    *req;
    int            nreq, *queue, qhead, qtail, inflight, completed, stop;
+   size_t         *reap;                  /* instances of evicted targets, to stop */
+   int            nreap, capreap;
    double         resident, peak, t0;
    int            loads, evictions;
 }SrvSct;
@@ -92,6 +94,64 @@ static double estimate(const SrvTarget *t)
    return (4.0 + 72.0 + 36.0) * t->nblk / 0.9 + 300.0 * t->nrow + 4e6;
 }
 
+static int load(SrvSct *s, SrvTarget *t);
+static void unload(SrvSct *s, SrvTarget *t);
+static int run_request(SrvTarget *t, GmlxRequest *r);
+
+/* One small mesh and one small system through every request kind, so that
+   the device context and the library's lazily loaded kernels are ready
+   before the first request: without it the requests of the first 0.2 s of a
+   run waited about 0.3 s, which was the whole p99 of a 2000-request trace. */
+static void warm_up(SrvSct *s)
+{
+   int nv = 0, nt = 0, nl = 0, nb = 0;
+   SrvTarget m, y;
+   GmlxRequest r;
+   float *crd;
+   int *tet, *ref, *lin = NULL, *col = NULL;
+   double *val = NULL, *rhs = NULL;
+
+   memset(&m, 0, sizeof(m));
+   memset(&y, 0, sizeof(y));
+   GmlxCubeSizes(4, &nv, &nt);
+   crd = malloc((size_t)nv * 16);
+   tet = malloc((size_t)nt * 16);
+   ref = calloc((size_t)nv, sizeof(int));
+   if(crd && tet && ref && GmlxCubeMesh(4, 1, 0.2, 1, crd, tet, ref))
+   {
+      m.kind = 0; m.nv = nv; m.nt = nt; m.crd = crd; m.tet = tet; m.ref = ref; m.h = 0.25;
+      if(load(s, &m))
+      {
+         memset(&r, 0, sizeof(r));
+         r.kind = GmlxReqQuality;
+         run_request(&m, &r);
+         r.kind = GmlxReqSmooth;
+         run_request(&m, &r);
+      }
+      unload(s, &m);
+   }
+   if(GmlxCubeSpdSizes(4, 0, &nl, &nb))
+   {
+      lin = malloc((size_t)(nl + 1) * sizeof(int));
+      col = malloc((size_t)nb * sizeof(int));
+      val = malloc((size_t)nb * 9 * sizeof(double));
+      rhs = malloc((size_t)nl * 3 * sizeof(double));
+      if(lin && col && val && rhs && GmlxCubeSpdMatrix(4, 0, 1, lin, col, val, rhs))
+      {
+         y.kind = 1; y.nrow = nl; y.nblk = nb; y.lin = lin; y.col = col; y.val = val; y.rhs = rhs;
+         if(load(s, &y))
+         {
+            memset(&r, 0, sizeof(r));
+            r.kind = GmlxReqSolve;
+            run_request(&y, &r);
+         }
+         unload(s, &y);
+      }
+   }
+   free(crd); free(tet); free(ref);
+   free(lin); free(col); free(val); free(rhs);
+}
+
 size_t GmlxServeNew(int dev, double BudgetBytes, int NmbSlot)
 {
    SrvSct *s;
@@ -103,6 +163,7 @@ size_t GmlxServeNew(int dev, double BudgetBytes, int NmbSlot)
    s->dev = dev;
    s->slots = NmbSlot;
    s->budget = BudgetBytes;
+   warm_up(s);
    return (size_t)s;
 }
 
@@ -232,7 +293,10 @@ static int run_request(SrvTarget *t, GmlxRequest *r)
 }
 
 /* make room for `need` bytes by evicting idle resident targets, least
-   recently used first; called with the lock held */
+   recently used first; called with the lock held.  An evicted instance is
+   handed to the reaper thread: stopping it frees pinned host memory, which
+   waits for all work on the device, and must not hold up the dispatcher or
+   the slots (they need the lock to take and finish requests). */
 static int reserve(SrvSct *s, double need)
 {
    while(s->resident + need > s->budget)
@@ -246,7 +310,14 @@ static int reserve(SrvSct *s, double need)
       }
       if(!v)
          return 0;
-      unload(s, v);
+      if(v->g && s->reap && s->nreap < s->capreap)
+      {
+         s->reap[ s->nreap++ ] = v->g;
+         v->g = 0;
+         pthread_cond_signal(&s->cv_reap);
+      }
+      else
+         unload(s, v);
       v->reserved = 0;
       s->resident -= v->bytes;
       s->evictions++;
@@ -297,6 +368,28 @@ static void *worker(void *arg)
       s->inflight--;
       s->completed++;
       pthread_cond_signal(&s->cv_done);
+   }
+   pthread_mutex_unlock(&s->mu);
+   return NULL;
+}
+
+/* stops the instances of evicted targets, outside the lock */
+static void *reaper(void *arg)
+{
+   SrvSct *s = (SrvSct *)arg;
+   pthread_mutex_lock(&s->mu);
+   for(;;)
+   {
+      while(!s->nreap && !s->stop)
+         pthread_cond_wait(&s->cv_reap, &s->mu);
+      if(!s->nreap)
+         break;
+      {
+         size_t g = s->reap[ --s->nreap ];
+         pthread_mutex_unlock(&s->mu);
+         GmlStop(g);
+         pthread_mutex_lock(&s->mu);
+      }
    }
    pthread_mutex_unlock(&s->mu);
    return NULL;
@@ -375,21 +468,33 @@ static int run_batching(SrvSct *s, GmlxRequest *req, int n)
    pthread_t th[SRV_MAXSLOT];
    int *pend = malloc((size_t)n * sizeof(int)), npend = 0, next = 0, i, nth = 0;
 
+   pthread_t rp;
+   int have_rp;
+
    s->queue = malloc((size_t)n * sizeof(int));
-   if(!pend || !s->queue)
+   s->capreap = s->ntg;
+   s->reap = malloc((size_t)(s->capreap ? s->capreap : 1) * sizeof(size_t));
+   s->nreap = 0;
+   if(!pend || !s->queue || !s->reap)
    {
       free(pend);
       free(s->queue);
+      free(s->reap);
       s->queue = NULL;
+      s->reap = NULL;
       return 0;
    }
    s->qhead = s->qtail = s->inflight = s->completed = s->stop = 0;
    pthread_mutex_init(&s->mu, NULL);
    pthread_cond_init(&s->cv_work, NULL);
    pthread_cond_init(&s->cv_done, NULL);
+   pthread_cond_init(&s->cv_reap, NULL);
    for(i=0;i<s->slots;i++)
       if(pthread_create(&th[nth], NULL, worker, s) == 0)
          nth++;
+   have_rp = pthread_create(&rp, NULL, reaper, s) == 0;
+   if(!have_rp)
+      s->capreap = 0;                     /* evictions stop instances in place */
 
    pthread_mutex_lock(&s->mu);
    while(s->completed < n)
@@ -448,15 +553,22 @@ static int run_batching(SrvSct *s, GmlxRequest *req, int n)
    }
    s->stop = 1;
    pthread_cond_broadcast(&s->cv_work);
+   pthread_cond_broadcast(&s->cv_reap);
    pthread_mutex_unlock(&s->mu);
    for(i=0;i<nth;i++)
       pthread_join(th[i], NULL);
+   if(have_rp)
+      pthread_join(rp, NULL);             /* it stops what is left to reap first */
    pthread_cond_destroy(&s->cv_work);
    pthread_cond_destroy(&s->cv_done);
+   pthread_cond_destroy(&s->cv_reap);
    pthread_mutex_destroy(&s->mu);
    free(pend);
    free(s->queue);
+   free(s->reap);
    s->queue = NULL;
+   s->reap = NULL;
+   s->nreap = s->capreap = 0;
    return nth > 0;
 }
 

@@ -284,7 +284,9 @@ typedef struct
 }GmlxServeStats;
 
 /* Server on device dev with a device-memory budget (bytes) for resident
-   targets and NmbSlot concurrent requests (1..64). */
+   targets and NmbSlot concurrent requests (1..64).  It runs a small mesh and
+   a small system through every request kind before returning (device
+   context and kernels loaded up front, a few hundred ms on a cold process). */
 size_t   GmlxServeNew         (int dev, double BudgetBytes, int NmbSlot);
 
 /* Register a tet mesh (crd 4 floats per vertex, ref per vertex or NULL;
