@@ -68,6 +68,9 @@ def parse():
     p.add_argument("--meshes", type=int, default=512, help="batch: number of meshes")
     p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     p.add_argument("--rate", type=float, default=200.0, help="serve: requests per second")
+    p.add_argument("--saturate", type=int, default=600,
+                   help="serve: requests of the trace replayed all at t = 0 on both paths "
+                        "(capacity)")
     p.add_argument("--serial-requests", type=int, default=200,
                    help="serve: requests of the trace replayed on the serial plain path")
     return p.parse_args()
@@ -692,7 +695,17 @@ def run_serve(args, dist):
 
     def bucket(x):
         return int(np.argmin(np.abs(logt - x)))
+    def register(server, cls, b):
+        if cls == 0:
+            crd, tet, ref = meshes[b]
+            return G.lib.GmlxServeAddMesh(server, len(crd), G.as_ptr(crd), G.as_ptr(ref),
+                                          len(tet), G.as_ptr(tet), 1.0 / ns[b])
+        lin, col, val, rhs = systems[b]
+        return G.lib.GmlxServeAddSystem(server, len(lin) - 1, len(col), G.as_ptr(lin),
+                                        G.as_ptr(col), G.as_ptr(val), G.as_ptr(rhs))
+
     srv = G.lib.GmlxServeNew(dist.local, 150e9, 8)
+    added = []
     nreq = int(args.rate * args.duration)
     req = (G.GmlxRequest * nreq)()
     seen = {0: [], 1: []}
@@ -707,14 +720,8 @@ def run_serve(args, dist):
             target = int(rng.choice(seen[cls]))
         else:
             b = bucket(rng.uniform(np.log(1e4), np.log(1e7)))
-            if cls == 0:
-                crd, tet, ref = meshes[b]
-                target = G.lib.GmlxServeAddMesh(srv, len(crd), G.as_ptr(crd), G.as_ptr(ref),
-                                                len(tet), G.as_ptr(tet), 1.0 / ns[b])
-            else:
-                lin, col, val, rhs = systems[b]
-                target = G.lib.GmlxServeAddSystem(srv, len(lin) - 1, len(col), G.as_ptr(lin),
-                                                  G.as_ptr(col), G.as_ptr(val), G.as_ptr(rhs))
+            target = register(srv, cls, b)
+            added.append((cls, b))
             seen[cls].append(target)
         req[i].kind, req[i].target, req[i].arrival = kind, target, t
         kinds.append(kind)
@@ -729,6 +736,26 @@ def run_serve(args, dist):
         ser[i].kind, ser[i].target, ser[i].arrival = req[i].kind, req[i].target, req[i].arrival
     sts = G.GmlxServeStats()
     G.lib.GmlxServeRun(srv, ser, nser, G.GmlxServeSerial, ctypes.byref(sts))
+    # capacity: the first --saturate requests of the trace all due at t = 0,
+    # through each path (requests/s the path sustains when never idle), on a
+    # second server with the same targets and none of them resident
+    nsat = min(nreq, args.saturate)
+    cap = {}
+    srv2 = G.lib.GmlxServeNew(dist.local, 150e9, 8)
+    for cls, b in added:
+        register(srv2, cls, b)
+    for mode, name in ((G.GmlxServeBatching, "batching"), (G.GmlxServeSerial, "serial")):
+        sat = (G.GmlxRequest * max(nsat, 1))()
+        for i in range(nsat):
+            sat[i].kind, sat[i].target, sat[i].arrival = req[i].kind, req[i].target, 0.0
+        stc = G.GmlxServeStats()
+        G.lib.GmlxServeRun(srv2, sat, nsat, mode, ctypes.byref(stc))
+        cap[name] = {"requests": nsat, "completed": stc.completed, "seconds": round(stc.seconds, 3),
+                     "throughput_rps": round(stc.throughput, 2)}
+    G.lib.GmlxServeFree(srv2)
+    if cap["serial"]["throughput_rps"] > 0:
+        cap["batching_over_serial"] = round(cap["batching"]["throughput_rps"]
+                                            / cap["serial"]["throughput_rps"], 2)
     def breakdown(reqs, n):
         """per kind: mean queueing delay (start - arrival) and service time
         (finish - start), split by whether the request loaded its target"""
@@ -775,6 +802,7 @@ def run_serve(args, dist):
                            "sizes_tets": [int(6 * n ** 3) for n in ns], "reuse": 0.5,
                            "budget_gb": 150, "slots": 8, "pool_generation_s": round(tgen, 1)},
                 "batching": d(stb), "batching_by_kind": bd, "serial_prefix": d(sts),
+                "capacity_saturated": cap,
                 "same_result_alone_and_in_mix": "%d of %d" % (same, nser), "clocks": clk}
         print(json.dumps(line), flush=True)
 
