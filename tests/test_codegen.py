@@ -10,7 +10,7 @@ import pytest
 from conftest import PARAMS
 
 KDIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "kernels")
-REF = os.environ.get("GML_REFERENCE_ROOT", "/root/reference")
+from oracle.build import REF_ROOT as REF  # noqa: E402  (where the reference tree lies)
 
 
 def body(name):

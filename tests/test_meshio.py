@@ -9,7 +9,7 @@ import os
 import numpy as np
 import pytest
 
-REF = os.environ.get("GML_REFERENCE_ROOT", "/root/reference")
+from oracle.build import REF_ROOT as REF  # noqa: E402  (where the reference tree lies)
 KW_VER, KW_EDG, KW_TRI, KW_TET = 4, 5, 6, 8
 
 
