@@ -16,6 +16,26 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "gml_device.h"
+
+/* block-sparse SpMV tuning: the k-loop unroll and the load used for the
+   matrix streams (column indices and values, read once per product).
+   Measured on the 96^3 cube system (FP32): no unrolling and evict-first
+   streaming loads (ld.global.cs) take the reference-API SpMV from 97.8 to
+   92.2 us and the CG's fused SpMV from 120.1 to 108.1 us; the streamed
+   matrix no longer pushes the just-written vectors out of L2, so the CG
+   update also drops from 27.0 to 22.7 us. */
+#ifndef SPMV_UNROLL
+#define SPMV_UNROLL 1
+#endif
+constexpr int kSpmvUnroll = SPMV_UNROLL;   /* pragma arguments are not macro-expanded */
+#ifndef SPMV_STREAM
+#define SPMV_STREAM 1
+#endif
+#if SPMV_STREAM
+#define SPMV_LDM(p) __ldcs(p)
+#else
+#define SPMV_LDM(p) __ldg(p)
+#endif
 #include "gml_linalg.h"
 
 #define LA_THREADS 256
@@ -65,10 +85,10 @@ sell_spmv_kernel(int n, const int64_t *__restrict__ soff, const int *__restrict_
    for(int i=0;i<B;i++)
       acc[i] = (T)0;
 
-#pragma unroll 2
+#pragma unroll kSpmvUnroll
    for(int k=0;k<d;k++)
    {
-      const int c = __ldg(cp + (size_t)k * 32);
+      const int c = SPMV_LDM(cp + (size_t)k * 32);
       T xv[XS];
       load_line<T, XS>(x + (size_t)c * XS, xv);
       const T *blk = vp + (size_t)k * (B * B * 32);
@@ -76,7 +96,7 @@ sell_spmv_kernel(int n, const int64_t *__restrict__ soff, const int *__restrict_
       for(int i=0;i<B;i++)
 #pragma unroll
          for(int j=0;j<B;j++)
-            acc[i] += __ldg(blk + (i * B + j) * 32) * xv[j];
+            acc[i] += SPMV_LDM(blk + (i * B + j) * 32) * xv[j];
    }
 
    T *yl = y + (size_t)r * ys;

@@ -33,6 +33,26 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "gml_device.h"
+
+/* block-sparse SpMV tuning: the k-loop unroll and the load used for the
+   matrix streams (column indices and values, read once per product).
+   Measured on the 96^3 cube system (FP32): no unrolling and evict-first
+   streaming loads (ld.global.cs) take the reference-API SpMV from 97.8 to
+   92.2 us and the CG's fused SpMV from 120.1 to 108.1 us; the streamed
+   matrix no longer pushes the just-written vectors out of L2, so the CG
+   update also drops from 27.0 to 22.7 us. */
+#ifndef SPMV_UNROLL
+#define SPMV_UNROLL 1
+#endif
+constexpr int kSpmvUnroll = SPMV_UNROLL;   /* pragma arguments are not macro-expanded */
+#ifndef SPMV_STREAM
+#define SPMV_STREAM 1
+#endif
+#if SPMV_STREAM
+#define SPMV_LDM(p) __ldcs(p)
+#else
+#define SPMV_LDM(p) __ldg(p)
+#endif
 #include "gml_solver.h"
 
 #define SV_THREADS 256
@@ -235,10 +255,10 @@ __device__ __forceinline__ void sv_row_product(int r, const int64_t *__restrict_
 #pragma unroll
    for(int i=0;i<VS;i++)
       y[i] = (T)0;
-#pragma unroll 2
+#pragma unroll kSpmvUnroll
    for(int k=0;k<d;k++)
    {
-      const int c = __ldg(cp + (size_t)k * 32);
+      const int c = SPMV_LDM(cp + (size_t)k * 32);
       T xv[VS];
       fetch((size_t)c, xv);
       const T *blk = vp + (size_t)k * (B * B * 32);
@@ -246,7 +266,7 @@ __device__ __forceinline__ void sv_row_product(int r, const int64_t *__restrict_
       for(int i=0;i<B;i++)
 #pragma unroll
          for(int j=0;j<B;j++)
-            y[i] += __ldg(blk + (i * B + j) * 32) * xv[j];
+            y[i] += SPMV_LDM(blk + (i * B + j) * 32) * xv[j];
    }
 }
 
