@@ -116,6 +116,13 @@ def build(force=False, verbose=False, defines=(), out=None, objdir=None):
             for o in outs:
                 if o.strip():
                     print(o)
+    # the cl2h tool of the CMake package (cmake/GMlibConfig.cmake, compile_cl)
+    cl2h_src = os.path.join(CSRC, "cl2h.c")
+    cl2h = os.path.join(PKG, "cl2h")
+    if out is None and (force or _stale(cl2h, [cl2h_src])):
+        jobs_host = [["gcc", "-O2", "-std=gnu11", "-Wall", cl2h_src, "-o", cl2h]]
+        for j in jobs_host:
+            _run(j)
     if jobs or force or not os.path.exists(lib):
         libdirs = _cuda_libdirs()
         link = [NVCC] + ARCH + ["-shared", "-o", lib] + objs
