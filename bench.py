@@ -189,9 +189,26 @@ def mesh(n):
     return crd, tet, ref
 
 
-def workload_config(n, nv, nt, wset_mb):
+def degree_summary(tets):
+    """Vertex -> tet degrees over one or more meshes: min, mean, max and the
+    histogram {degree: vertices}."""
+    hist = np.zeros(1, np.int64)
+    for t in tets:
+        d = np.bincount(np.bincount(np.asarray(t).ravel()))
+        if len(d) > len(hist):
+            hist = np.pad(hist, (0, len(d) - len(hist)))
+        hist[:len(d)] += d
+    hist[0] = 0
+    degs = np.nonzero(hist)[0]
+    return {"min": int(degs[0]), "max": int(degs[-1]),
+            "mean": round(float((degs * hist[degs]).sum() / hist[degs].sum()), 3),
+            "hist": {str(int(k)): int(hist[k]) for k in degs}}
+
+
+def workload_config(n, nv, nt, wset_mb, degrees=None):
     return {"workload": "ball-of-points Laplacian smoothing + mean-ratio quality, "
                         "%d^3-hex cube, reflected 6-tet split" % n,
+            "vertex_tet_degrees": degrees,
             "hex_per_side": n, "tets": nt, "vertices": nv, "sweeps_per_step": SWEEPS,
             "per_sweep": "Jacobi sweep (boundary fixed) + quality, 64-bin histogram, "
                          "min/argmin, FP64 inverted flags",
@@ -249,7 +266,7 @@ def run_reference(args, dist):
             "ms_per_step": round(per * SWEEPS * 1e3, 3), "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(n, len(crd), len(tet), wset),
+            "config": workload_config(n, len(crd), len(tet), wset, degree_summary([tet])),
             "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads,
                              "kind": "port", "sample": sample},
             "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
@@ -269,6 +286,7 @@ def run_gpu(args, dist):
     dev = dist.local
     crd, tet, ref = mesh(n)
     nv, nt = len(crd), len(tet)
+    degrees = degree_summary([tet])
 
     g = G.lib.GmlInit(dev)
     if not g:
@@ -372,7 +390,7 @@ def run_gpu(args, dist):
                 "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": round(per_step * 1e3, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": workload_config(n, nv, nt, wset),
+                "config": workload_config(n, nv, nt, wset, degrees),
                 "gpu_launches": args.steps * (2 * SWEEPS + 1),
                 "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
                 "result_check": {"last_sweep_min_quality": last.MinQal,
@@ -608,6 +626,7 @@ def run_batch(args, dist):
     tgen = time.time() - t0
     nv = np.array([len(m[0]) for m in ms], np.int32)
     nt = np.array([len(m[1]) for m in ms], np.int32)
+    degrees = degree_summary([m[1] for m in ms])
     h = 1.0 / ns.astype(np.float64)
     g = G.lib.GmlInit(dist.local)
     G.lib.GmlxSetTiming(g, 0)
@@ -656,6 +675,7 @@ def run_batch(args, dist):
                 "config": {"workload": "%d jittered tet cubes, hexes per side log-uniform in "
                                        "[10, 80], reflected split" % len(ms),
                            "tets": int(nt.sum()), "vertices": int(nv.sum()), "sweeps": sweeps,
+                           "vertex_tet_degrees": degrees,
                            "generation_s": round(tgen, 1)},
                 "queue": out["queue"], "loop": out["loop"],
                 "speedup_vs_loop": round(out["loop"]["ms_per_run"] / out["queue"]["ms_per_run"], 2),
@@ -800,7 +820,8 @@ def run_serve(args, dist):
                 "config": {"workload": "Poisson %.0f req/s for %.0f s, 50/30/20 quality / "
                                        "10-sweep smoothing / CG (1e-10)" % (args.rate, args.duration),
                            "sizes_tets": [int(6 * n ** 3) for n in ns], "reuse": 0.5,
-                           "budget_gb": 150, "slots": 8, "pool_generation_s": round(tgen, 1)},
+                           "budget_gb": 150, "slots": 8, "pool_generation_s": round(tgen, 1),
+                           "vertex_tet_degrees": degree_summary([m[1] for m in meshes])},
                 "batching": d(stb), "batching_by_kind": bd, "serial_prefix": d(sts),
                 "capacity_saturated": cap,
                 "same_result_alone_and_in_mix": "%d of %d" % (same, nser), "clocks": clk}
