@@ -60,11 +60,12 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--workload", default="smooth",
-                   choices=["smooth", "solve", "batch", "serve", "p2"],
-                   help="smooth: the smoothing + quality step (default); solve: block SpMV "
-                        "and CG; batch: 512 meshes through the tile queue vs the per-mesh "
-                        "launch loop; serve: the request loop on a Poisson stream; p2: the "
-                        "P2Quality flow through a generated kernel")
+                   choices=["smooth", "quality", "solve", "batch", "serve", "p2"],
+                   help="smooth: the smoothing + quality step (default); quality: the plain "
+                        "quality pass on the 32^3-hex Kuhn cube; solve: block SpMV and CG; "
+                        "batch: 512 meshes through the tile queue vs the per-mesh launch loop; "
+                        "serve: the request loop on a Poisson stream; p2: the P2Quality flow "
+                        "through a generated kernel")
     p.add_argument("--meshes", type=int, default=512, help="batch: number of meshes")
     p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     p.add_argument("--rate", type=float, default=200.0, help="serve: requests per second")
@@ -502,9 +503,150 @@ def gen_meshes(specs):
         return list(ex.map(one, specs))
 
 
+# ---------------------------------------------------- plain tet quality (C1)
+
+Q_N, Q_JITTER, Q_SEED = 32, 0.25, 12345
+
+
+def run_quality(args, dist):
+    """The plain tet-quality configuration: 32^3-hex cube, Kuhn split
+    (196,608 tets, 35,937 vertices), interior vertices jittered by +-0.25h
+    (seed 12345), Hilbert order.  One pass computes the mean-ratio quality of
+    every tet with min/argmin, max/argmax, the sum, the 64-bin histogram and
+    the FP64-decided inverted flags (GmlxQualityStats).
+    value: tets/s of the pass, CUDA events around each launch, with the L2
+    flushed between launches by scaling a 256 MB vector (the mesh alone,
+    4.5 MB, would stay in the 129 MB L2).  The same measure written as a
+    user body, compiled by GmlCompileKernel and reduced by GmlxReduceArg, is
+    reported beside it.  e2e: coordinates up, the pass, the statistics down,
+    through the C ABI with host buffers.  CPU: the FP64 serial oracle on one
+    core."""
+    import gmlib_gb300 as G
+    n = args.n if args.n != N_HEX else Q_N
+    crd, tet, ref = G.cube_mesh(n, split=0, jitter=Q_JITTER, seed=Q_SEED)
+    nv, nt = len(crd), len(tet)
+    h = 1.0 / n
+    g = G.lib.GmlInit(dist.local)
+    if not g:
+        raise SystemExit("GmlInit failed")
+    G.lib.GmlxSetTiming(g, 0)
+    G.lib.GmlNewParameters(g, len(P2_PARAMS), P2_PARAMS)
+    v, t = G.upload_mesh(g, crd, tet, ref)
+    if G.lib.GmlxMeshSetup(g, 1) != 1:
+        raise SystemExit("GmlxMeshSetup failed")
+    flush = G.lib.GmlNewVector(g, 16 << 20, 4, None, G.GmlFlt)     # 256 MB
+    one = ctypes.c_double(1.0)
+    res = G.GmlxQuality()
+
+    def timed(launch, k):
+        e0, e1 = G.lib.GmlxEventCreate(), G.lib.GmlxEventCreate()
+        tot = 0.0
+        for _ in range(k):
+            G.lib.GmlScaleVec(g, flush, ctypes.byref(one))
+            G.lib.GmlxEventRecord(g, e0)
+            launch()
+            G.lib.GmlxEventRecord(g, e1)
+            tot += G.lib.GmlxEventElapsed(e0, e1)
+        return tot / k
+
+    def native():
+        G.lib.GmlxQualityStats(g, h, 0, None)
+
+    for _ in range(max(args.warmup, 3)):
+        native()
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    clocks.start()
+    per = dist.max(timed(native, args.steps))
+    clk = clocks.stop()
+    if G.lib.GmlxQualityStats(g, h, 0, ctypes.byref(res)) != 1:
+        raise SystemExit("GmlxQualityStats failed")
+
+    # the same measure as a user body through the reference API
+    qidx = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 1, G.GmlFlt, b"qal")
+    k = G.compile_kernel(g, G.mean_ratio_body(), "mean_ratio", G.GmlTetrahedra,
+                         [(v, G.GmlReadMode, 0), (qidx, G.GmlWriteMode, 0)])
+    if not k:
+        raise SystemExit("mean-ratio body did not compile")
+    for _ in range(max(args.warmup, 3) + 8):            # block-size calibration included
+        G.lib.GmlLaunchKernel(g, k)
+    per_gen = dist.max(timed(lambda: G.lib.GmlLaunchKernel(g, k), args.steps))
+    mn, mx = ctypes.c_float(), ctypes.c_float()
+    imn, imx = ctypes.c_int(), ctypes.c_int()
+    G.lib.GmlxReduceArg(g, qidx, ctypes.byref(mn), ctypes.byref(imn), ctypes.byref(mx),
+                        ctypes.byref(imx))
+    tr = []
+    for i in range(args.steps + 3):
+        ts = time.perf_counter()
+        G.lib.GmlLaunchKernel(g, k)
+        G.lib.GmlxReduceArg(g, qidx, ctypes.byref(mn), ctypes.byref(imn), ctypes.byref(mx),
+                            ctypes.byref(imx))
+        if i >= 3:
+            tr.append(time.perf_counter() - ts)
+
+    # end to end: coordinates up, the pass, the statistics down
+    host_crd = np.ascontiguousarray(crd)
+    e2e_t = []
+    for i in range(args.e2e_steps + 2):
+        ts = time.perf_counter()
+        G.lib.GmlxSetData(g, v, G.as_ptr(host_crd), host_crd.nbytes)
+        G.lib.GmlxQualityStats(g, h, 0, ctypes.byref(res))
+        if i >= 2:
+            e2e_t.append(time.perf_counter() - ts)
+    e2e_s = dist.max(statistics.median(e2e_t))
+    G.lib.GmlStop(g)
+
+    byts = 16.0 * nt + 16.0 * nv + 4.0 * ((nt + 31) // 32)
+    peak, peak_src = peak_hbm()
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        import oracle as O
+        ts_ = []
+        for _ in range(4):
+            ts = time.perf_counter()
+            q, _, _, _ = O.quality_stats(crd, tet)
+            int(np.argmin(q)), int(np.argmax(q))
+            ts_.append(time.perf_counter() - ts)
+        tc = statistics.median(ts_[1:])
+        cpu = {"value": round(nt / tc / 1e6, 3), "unit": "M tets/s", "cores": 1, "kind": "port",
+               "sample": "FP64 serial oracle (quality, histogram, flags, argmin/argmax) on the "
+                         "whole mesh, median of 3 after 1 warm-up"}
+    if dist.rank == 0:
+        line = {"metric": "tet qualities per second (quality + min/max/argmin pass)",
+                "value": round(dist.world * nt / per / 1e6, 2), "unit": "M tets/s",
+                "n_gpus": dist.world, "steps": args.steps, "warmup": max(args.warmup, 3),
+                "ms_per_step": round(per * 1e3, 5), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "mean-ratio quality + min/max/argmin, %d^3-hex cube, "
+                                       "Kuhn split" % n,
+                           "tets": nt, "vertices": nv, "jitter": Q_JITTER, "seed": Q_SEED,
+                           "l2": "flushed between launches (256 MB vector scale); the mesh "
+                                 "(%.1f MB) is smaller than L2" % (byts / 1e6)},
+                "gpu_launches": 2 * args.steps,
+                "roofline": {"bound": "hbm", "kernel": "tet_quality_tma_kernel",
+                             "achieved": round(byts / per / 1e9, 1), "peak": peak, "unit": "GB/s",
+                             "frac": round(byts / per / 1e9 / peak, 4), "traffic": None,
+                             "algorithmic_bytes_per_launch": byts,
+                             "mean_launch_us": round(per * 1e6, 2), "peak_source": peak_src,
+                             "note": "a 4.5 MB pass is latency-bound; the fraction is context"},
+                "generated": {"kernel": "gmlib_gb300/kernels/mean_ratio.cl via GmlCompileKernel",
+                              "mean_launch_us": round(per_gen * 1e6, 2),
+                              "launch_plus_reduce_arg_us": round(statistics.median(tr) * 1e6, 1),
+                              "min": mn.value, "argmin": imn.value},
+                "e2e": {"value": round(dist.world * nt / e2e_s / 1e6, 2), "unit": "M tets/s",
+                        "h2d_bytes_per_step": host_crd.nbytes,
+                        "d2h_bytes_per_step": ctypes.sizeof(G.GmlxQuality),
+                        "ms_per_step": round(e2e_s * 1e3, 4)},
+                "cpu_baseline": cpu, "clocks": clk,
+                "result_check": {"min": res.MinQal, "argmin": res.MinIdx, "max": res.MaxQal,
+                                 "argmax": res.MaxIdx, "inverted": res.NmbInv,
+                                 "generated_argmin_agrees": imn.value == res.MinIdx}}
+        print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------- P2 quality
 
-P2_FLOPS = 1612.0          # flops per P2 tet, as counted by examples/P2Quality
+P2_FLOPS = 1612.0         # flops per P2 tet, as counted by examples/P2Quality
 P2_PARAMS = b"typedef struct {\n   int   foo;\n   float res;\n}GmlParSct;\n"
 
 
@@ -842,6 +984,8 @@ def main():
             run_serve(args, dist)
         elif args.workload == "p2":
             run_p2(args, dist)
+        elif args.workload == "quality":
+            run_quality(args, dist)
         else:
             run_gpu(args, dist)
     finally:

@@ -262,6 +262,13 @@ def p2_body():
         return f.read()
 
 
+def mean_ratio_body():
+    """The mean-ratio tetrahedron quality as a GMlib-dialect kernel body
+    (kernels/mean_ratio.cl): reads VerCrd[4], writes qal."""
+    with open(os.path.join(_HERE, "kernels", "mean_ratio.cl"), "rb") as f:
+        return f.read()
+
+
 def compile_kernel(g, src, name, msh, dats):
     """dats: list of (index, flags, link) triplets."""
     n = len(dats)

@@ -181,6 +181,19 @@ def test_p2_downlink_naming_contract(G, offline):
         assert "MidCrd[%d] =  MidCrdTab[ TetEdgLnk.s%d ]" % (j, j) in s
 
 
+def test_mean_ratio_body_compiles(G, offline):
+    """The package's mean-ratio body reads VerCrd through TetVer and writes
+    one float per tet."""
+    g = offline
+    crd, tet, v, t = mesh(G, g)
+    q = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 1, G.GmlFlt, b"qal")
+    k = G.compile_kernel(g, G.mean_ratio_body(), "mean_ratio", G.GmlTetrahedra,
+                         [(v, G.GmlReadMode, 0), (q, G.GmlWriteMode, 0)])
+    assert k
+    s = source(G, g, k)
+    assert "float4 VerCrd[4];" in s and "qalTab[ cnt + count.s1 ] = qal;" in s
+
+
 @pytest.mark.parametrize("kernel,msh,spec", [
     ("MeshQuality/compute_quality.cl", "tet", "quality"),
     ("NodeSmoothing/scatter.cl", "tet", "scatter"),

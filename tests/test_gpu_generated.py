@@ -92,6 +92,35 @@ def test_p2_quality_matches_golden(G, gpu):
     assert np.all(np.abs(qg - gd["quality"]) <= P2_ATOL + P2_RTOL * np.abs(gd["quality"]))
 
 
+@pytest.mark.parametrize("n,split,jitter", [(32, 0, 0.25), (12, 1, 0.45)])
+def test_mean_ratio_body_matches_oracle_and_native(G, O, gpu, n, split, jitter):
+    """The mean-ratio dialect body against the FP64 oracle (signed by the
+    FP64 determinant) and against the native quality pass: the same values
+    within 2e-5, the same sign wherever the FP32 determinant is not within
+    its rounding error of zero, and the same argmin when the minimum is
+    isolated."""
+    crd, tet, ref = G.cube_mesh(n, split=split, jitter=jitter, seed=n)
+    v, t = setup_mesh(G, gpu, crd, tet, ref)
+    q = G.lib.GmlNewSolutionData(gpu, G.GmlTetrahedra, 1, G.GmlFlt, b"qal")
+    k = G.compile_kernel(gpu, G.mean_ratio_body(), "mean_ratio", G.GmlTetrahedra,
+                         [(v, G.GmlReadMode, 0), (q, G.GmlWriteMode, 0)])
+    assert k and G.lib.GmlLaunchKernel(gpu, k) == 1
+    qg = G.get_data(gpu, q, np.float32, len(tet)).astype(np.float64)
+    qo, _, _, _ = O.quality_stats(crd, tet)
+    near_flat = np.abs(qo) < 1e-4
+    assert np.all(np.abs(np.abs(qg) - np.abs(qo)) <= 2e-5)
+    assert np.array_equal(np.sign(qg[~near_flat]), np.sign(qo[~near_flat]))
+    assert G.lib.GmlxMeshSetup(gpu, 1) == 1
+    res = G.GmlxQuality()
+    assert G.lib.GmlxQualityStats(gpu, 1.0 / n, 0, ctypes.byref(res)) == 1
+    srt = np.sort(qo)
+    if srt[1] - srt[0] > 1e-4:
+        fmin, imin, fmax, imax = ctypes.c_float(), ctypes.c_int(), ctypes.c_float(), ctypes.c_int()
+        assert G.lib.GmlxReduceArg(gpu, q, ctypes.byref(fmin), ctypes.byref(imin),
+                                   ctypes.byref(fmax), ctypes.byref(imax)) == 1
+        assert imin.value == res.MinIdx == int(np.argmin(qo))
+
+
 def test_reductions_match_oracle(G, O, gpu):
     crd, tet, ref = G.cube_mesh(32, split=0, jitter=0.25, seed=5)
     v, t = setup_mesh(G, gpu, crd, tet, ref)

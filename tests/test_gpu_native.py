@@ -60,7 +60,7 @@ def check_stats(O, crd, tet, res, h):
     return q, flags
 
 
-@pytest.mark.parametrize("n,split,jitter", [(16, 0, 0.25), (14, 1, 0.45)])
+@pytest.mark.parametrize("n,split,jitter", [(16, 0, 0.25), (14, 1, 0.45), (45, 1, 0.3)])
 def test_quality_stats_match_oracle(G, O, gpu, n, split, jitter):
     crd, tet, ref, v, t = make(G, gpu, n, split, jitter, 5, 1)
     qidx = G.lib.GmlNewSolutionData(gpu, G.GmlTetrahedra, 1, G.GmlFlt, b"q")
