@@ -60,9 +60,10 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--workload", default="smooth",
-                   choices=["smooth", "quality", "solve", "batch", "serve", "p2"],
+                   choices=["smooth", "quality", "nodesmooth", "solve", "batch", "serve", "p2"],
                    help="smooth: the smoothing + quality step (default); quality: the plain "
-                        "quality pass on the 32^3-hex Kuhn cube; solve: block SpMV and CG; "
+                        "quality pass on the 32^3-hex Kuhn cube; nodesmooth: the reference's "
+                        "NodeSmoothing flow through generated kernels; solve: block SpMV and CG; "
                         "batch: 512 meshes through the tile queue vs the per-mesh launch loop; "
                         "serve: the request loop on a Poisson stream; p2: the P2Quality flow "
                         "through a generated kernel")
@@ -644,6 +645,127 @@ def run_quality(args, dist):
         print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------- NodeSmoothing flow (reference API)
+
+def kernel_body(name):
+    with open(os.path.join(ROOT, "tests", "kernels", name), "rb") as f:
+        return f.read()
+
+
+def run_nodesmooth(args, dist):
+    """The reference's NodeSmoothing example flow through the reference API on
+    the smoothing mesh (128^3-hex cube, reflected split): the tet quality
+    body and a sum reduction, then 10 x (scatter: 4 optimal apex points per
+    tet; gather: mean of the ball's points facing each vertex through the
+    vertex -> tet ball with voyeurs, 0.2 relaxation; sum of the squared
+    moves), then the quality and its sum again.  Each GmlReduceVector
+    returns its value to the host, as in the example.  The bodies are this
+    repository's restatements of the example's scatter, gather and quality
+    kernels (tests/kernels).
+    value: algorithmic bytes of the flow / wall time of the flow (GB/s);
+    per-kernel device times with CUDA events over back-to-back launches."""
+    import gmlib_gb300 as G
+    n = args.n
+    crd, tet, ref = mesh(n)
+    nv, nt = len(crd), len(tet)
+    g = G.lib.GmlInit(dist.local)
+    if not g:
+        raise SystemExit("GmlInit failed")
+    G.lib.GmlxSetTiming(g, 0)
+    G.lib.GmlNewParameters(g, len(P2_PARAMS), P2_PARAMS)
+    v, t = G.upload_mesh(g, crd, tet, ref)
+    qal = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 1, G.GmlFlt, b"qal")
+    opt = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 4, G.GmlFlt4, b"OptCrd")
+    res = G.lib.GmlNewSolutionData(g, G.GmlVertices, 1, G.GmlFlt, b"res")
+    kq = G.compile_kernel(g, kernel_body("tet_quality.cl"), "quality", G.GmlTetrahedra,
+                          [(v, G.GmlReadMode, 0), (qal, G.GmlWriteMode, 0)])
+    ks = G.compile_kernel(g, kernel_body("optimal_points.cl"), "scatter", G.GmlTetrahedra,
+                          [(v, G.GmlReadMode, 0), (opt, G.GmlWriteMode, 0)])
+    kg = G.compile_kernel(g, kernel_body("relax_to_points.cl"), "gather", G.GmlVertices,
+                          [(res, G.GmlWriteMode, 0), (opt, G.GmlReadMode | G.GmlVoyeurs, 0),
+                           (v, G.GmlReadMode | G.GmlWriteMode, 0)])
+    if not (kq and ks and kg):
+        raise SystemExit("NodeSmoothing bodies did not compile")
+    host_crd = np.ascontiguousarray(crd)
+
+    def flow():
+        G.lib.GmlLaunchKernel(g, kq)
+        q0 = G.reduce(g, qal, G.GmlSum)
+        r = 0.0
+        for _ in range(10):
+            G.lib.GmlLaunchKernel(g, ks)
+            G.lib.GmlLaunchKernel(g, kg)
+            r = G.reduce(g, res, G.GmlSum)
+        G.lib.GmlLaunchKernel(g, kq)
+        return q0, r, G.reduce(g, qal, G.GmlSum)
+
+    for _ in range(max(args.warmup, 3)):          # includes the block-size calibration
+        G.lib.GmlxSetData(g, v, G.as_ptr(host_crd), host_crd.nbytes)
+        flow()
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    clocks.start()
+    walls = []
+    for _ in range(args.steps):
+        G.lib.GmlxSetData(g, v, G.as_ptr(host_crd), host_crd.nbytes)
+        G.lib.GmlxSynchronize(g)
+        ts = time.perf_counter()
+        q0, r, q1 = flow()
+        walls.append(time.perf_counter() - ts)
+    clk = clocks.stop()
+    wall = dist.max(statistics.median(walls))
+
+    # per-kernel device times, back-to-back launches on the instance's stream
+    e0, e1 = G.lib.GmlxEventCreate(), G.lib.GmlxEventCreate()
+    per = {}
+    for name, k in (("scatter", ks), ("gather", kg), ("quality", kq)):
+        G.lib.GmlxEventRecord(g, e0)
+        for _ in range(20):
+            G.lib.GmlLaunchKernel(g, k)
+        G.lib.GmlxEventRecord(g, e1)
+        per[name] = dist.max(G.lib.GmlxEventElapsed(e0, e1) / 20)
+    blk = {name: G.lib.GmlxKernelBlockSize(g, k) for name, k in
+           (("scatter", ks), ("gather", kg), ("quality", kq))}
+    regs = {name: G.lib.GmlxKernelRegisters(g, k) for name, k in
+            (("scatter", ks), ("gather", kg), ("quality", kq))}
+    G.lib.GmlStop(g)
+
+    # algorithmic bytes: scatter 16T (tets) + 16V (coordinates) + 64T (points
+    # out); gather 16T (ball entries) + 4V (degrees) + 64T (points in) + 32V
+    # (coordinates in and out) + 4V (res); quality 16T + 16V + 4T; sums 4 per line
+    kb = {"scatter": 80.0 * nt + 16.0 * nv, "gather": 80.0 * nt + 40.0 * nv,
+          "quality": 20.0 * nt + 16.0 * nv}
+    flow_bytes = 10 * (kb["scatter"] + kb["gather"] + 4.0 * nv) + 2 * (kb["quality"] + 4.0 * nt)
+    peak, peak_src = peak_hbm()
+    kern = {k: {"mean_launch_us": round(per[k] * 1e6, 2), "block": blk[k], "registers": regs[k],
+                "algorithmic_bytes": kb[k], "achieved": round(kb[k] / per[k] / 1e9, 1),
+                "frac": round(kb[k] / per[k] / 1e9 / peak, 4)} for k in per}
+    if dist.rank == 0:
+        line = {"metric": "NodeSmoothing flow through the reference API, GB/s",
+                "value": round(dist.world * flow_bytes / wall / 1e9, 1), "unit": "GB/s",
+                "n_gpus": dist.world, "steps": args.steps, "warmup": max(args.warmup, 3),
+                "ms_per_step": round(wall * 1e3, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "NodeSmoothing example flow (quality + sum, 10 x "
+                                       "(scatter, gather, residual sum), quality + sum), "
+                                       "%d^3-hex cube, reflected split" % n,
+                           "tets": nt, "vertices": nv, "vertex_tet_degrees": degree_summary([tet]),
+                           "l2": "inputs larger than L2 (OptCrd alone is %.0f MB)" % (64e-6 * nt),
+                           "step": "wall clock of the flow, host reductions included; the "
+                                   "coordinates are re-uploaded before each step, outside it"},
+                "gpu_launches": args.steps * (22 + 12),
+                "roofline": {"bound": "hbm", "kernel": "gather (generated)",
+                             "achieved": kern["gather"]["achieved"], "peak": peak, "unit": "GB/s",
+                             "frac": kern["gather"]["frac"], "traffic": None,
+                             "algorithmic_bytes_per_launch": kb["gather"],
+                             "mean_launch_us": kern["gather"]["mean_launch_us"],
+                             "peak_source": peak_src},
+                "kernels": kern, "clocks": clk,
+                "result_check": {"mean_quality_before": q0 / nt, "mean_quality_after": q1 / nt,
+                                 "last_residual": r}}
+        print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------- P2 quality
 
 P2_FLOPS = 1612.0         # flops per P2 tet, as counted by examples/P2Quality
@@ -986,6 +1108,8 @@ def main():
             run_p2(args, dist)
         elif args.workload == "quality":
             run_quality(args, dist)
+        elif args.workload == "nodesmooth":
+            run_nodesmooth(args, dist)
         else:
             run_gpu(args, dist)
     finally:

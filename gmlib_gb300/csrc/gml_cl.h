@@ -478,37 +478,80 @@ template<class T, int NI> struct gml_up_row
    GML_FN const T operator[](int j) const { return ok ? p[j] : gml_zero<T>(); }
 };
 
-template<class T, int NI> struct gml_up
+/* The ball row of the current entity: its codes (element << 4) | local
+   index, read through the row object shared by the entity's accessors.
+   With V = 4 the row is read in 16-byte pieces, kept in registers while a
+   loop walks through them: one load serves four consecutive codes, where
+   one load per code and per accessor touched the same 128-byte line of
+   every lane's row again and again.  Codes at or beyond the degree are the
+   table's zero padding and are returned without a load.  V = 1 reads one
+   code at a time (rows whose width is not a multiple of four codes). */
+template<int V> struct gml_balrow;
+
+struct __align__(16) gml_codes4 { int a, b, c, d; };
+
+template<> struct gml_balrow<4>
+{
+   const int *row;
+   int deg;
+   int q;               /* index of the piece held in c, -1 for none */
+   gml_codes4 c;
+   GML_FN int code(int k)
+   {
+      if(k >= deg)
+         return 0;
+      const int p = k >> 2;
+      if(p != q)
+      {
+         c = *(const gml_codes4 *)(row + 4 * p);
+         q = p;
+      }
+      const int e = k & 3;
+      return e == 0 ? c.a : e == 1 ? c.b : e == 2 ? c.c : c.d;
+   }
+};
+
+template<> struct gml_balrow<1>
+{
+   const int *row;
+   int deg;
+   GML_FN int code(int k) { return k < deg ? row[k] : 0; }
+};
+
+/* Uplinked datatype with NI items per line: X[k][j] is XTab[ball_k][j]
+   when k < deg, else the null value. */
+template<class T, int NI, int V> struct gml_up
 {
    const T (*tab)[NI];
-   const int *bal;      /* first code of this entity's ball row: (element << 4) | local index */
+   gml_balrow<V> *row;
    int deg;
    GML_FN gml_up_row<T,NI> operator[](int k) const
    {
       gml_up_row<T,NI> r;
       r.ok = k < deg;
-      r.p = tab[r.ok ? (bal[k] >> 4) : 0];
+      r.p = tab[r.ok ? (row->code(k) >> 4) : 0];
       return r;
    }
 };
 
 /* Uplinked datatype with one item per line: X[k] is XTab[ball_k] or null. */
-template<class T> struct gml_up1
+template<class T, int V> struct gml_up1
 {
    const T *tab;
-   const int *bal;
+   gml_balrow<V> *row;
    int deg;
    GML_FN const T operator[](int k) const
    {
-      return k < deg ? tab[bal[k] >> 4] : gml_zero<T>();
+      return k < deg ? tab[row->code(k) >> 4] : gml_zero<T>();
    }
 };
 
-/* Voyeurs: local index (0..7) of the looping entity inside ball element k. */
-struct gml_voy
+/* Voyeurs: local index (0..7) of the looping entity inside ball element k
+   (0 beyond the degree, the value of the table's padding). */
+template<int V> struct gml_voy
 {
-   const int *bal;
-   GML_FN char operator[](int k) const { return (char)(bal[k] & 7); }
+   gml_balrow<V> *row;
+   GML_FN char operator[](int k) const { return (char)(row->code(k) & 7); }
 };
 
 /* Ball link vector j of the current row, already shifted right by 4. */

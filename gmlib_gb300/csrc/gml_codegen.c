@@ -71,12 +71,41 @@ static int lazy_data(const GmlArgSct *a, const GmlArgSct *cpt, int lazy)
    return lazy && cpt && (a->FlgTab & GmlReadMode) && is_read_only(a);
 }
 
+/* The row object <link>Row that the lazy accessors of one ball link share
+   (gml_balrow in gml_cl.h), declared once before its first user.  Rows
+   whose width is a multiple of four codes are read in 16-byte pieces
+   (V = 4), others one code at a time (V = 1).  Its degree is the count of
+   a datatype uplinked through this link, else the row width.  Returns V. */
+static int ensure_row(Out *o, const GmlArgSct *ArgTab, int NmbArg, int li, int *RowDone)
+{
+   const GmlArgSct *l = &ArgTab[li];
+   const int W = GmlTypVecSiz[ l->ItmTyp ] * l->NmbItm, V = (W % 4) ? 1 : 4;
+   const char *deg = NULL;
+   char DegStr[16];
+   int j;
+
+   if(RowDone[li])
+      return RowDone[li];
+   for(j=0;j<NmbArg && !deg;j++)
+      if(ArgTab[j].LnkIdx == li && ArgTab[j].CntIdx != -1)
+         deg = ArgTab[ ArgTab[j].CntIdx ].nam;
+   if(!deg)
+   {
+      snprintf(DegStr, sizeof(DegStr), "%d", W);
+      deg = DegStr;
+   }
+   emit(o, "   gml_balrow<%d> %sRow = { (const int *)(%sTab + cnt), %s%s };\n",
+        V, l->nam, l->nam, deg, V == 4 ? ", -1" : "");
+   RowDone[li] = V;
+   return V;
+}
+
 int gml_generate(char **res, const char *PrcNam, int MshTyp, int NmbArg,
                  const GmlArgSct *ArgTab, const char *KrnSrc, const char *UsrTlk,
                  const char *ParSrc, int lazy)
 {
    Out o;
-   int i, j, k, l;
+   int i, j, k, l, V;
    char *tmp;
 
    o.cap = 16384;
@@ -258,6 +287,8 @@ int gml_generate(char **res, const char *PrcNam, int MshTyp, int NmbArg,
 
    /* ---------------- lazy accessors ---------------- */
    if(lazy)
+   {
+      int RowDone[ GML_MAXARG ] = { 0 };
       for(i=0;i<NmbArg;i++)
       {
          const GmlArgSct *a = &ArgTab[i];
@@ -274,21 +305,26 @@ int gml_generate(char **res, const char *PrcNam, int MshTyp, int NmbArg,
             emit(&o, "   %s %sDeg = %s;\n", GmlOclTypStr[ cpt->ItmTyp ], a->nam, cpt->nam);
             emit(&o, "   %s %sNul = gml_zero<%s>();\n", T, a->nam, T);
             emit(&o, "   #define   %sDegMax %d\n", a->nam, lnk->MaxDeg);
+            V = ensure_row(&o, ArgTab, NmbArg, a->LnkIdx, RowDone);
             if(a->NmbItm > 1)
-               emit(&o, "   const gml_up<%s,%d> %s = { %sTab, (const int *)(%sTab + cnt), %sDeg };\n",
-                    T, a->NmbItm, a->nam, a->nam, lnk->nam, a->nam);
+               emit(&o, "   const gml_up<%s,%d,%d> %s = { %sTab, &%sRow, %sDeg };\n",
+                    T, a->NmbItm, V, a->nam, a->nam, lnk->nam, a->nam);
             else
-               emit(&o, "   const gml_up1<%s> %s = { %sTab, (const int *)(%sTab + cnt), %sDeg };\n",
-                    T, a->nam, a->nam, lnk->nam, a->nam);
+               emit(&o, "   const gml_up1<%s,%d> %s = { %sTab, &%sRow, %sDeg };\n",
+                    T, V, a->nam, a->nam, lnk->nam, a->nam);
          }
          else if(a->LnkDir == 1 && a->NmbItm > 1 && (a->FlgTab & GmlReadMode))
          {
             /* ball row as link vectors shifted on access */
             emit(&o, "   const gml_ballink<%s> %s = { (const %s *)(%sTab + cnt) };\n", T, a->nam, T, a->nam);
             if(a->FlgTab & GmlVoyeurs)
-               emit(&o, "   const gml_voy %s = { (const int *)(%sTab + cnt) };\n", a->VoyNam, a->nam);
+            {
+               V = ensure_row(&o, ArgTab, NmbArg, i, RowDone);
+               emit(&o, "   const gml_voy<%d> %s = { &%sRow };\n", V, a->VoyNam, a->nam);
+            }
          }
       }
+   }
 
    /* ---------------- user body ---------------- */
    tmp = gml_rewrite_opencl(KrnSrc);

@@ -72,8 +72,8 @@ def test_uplink_voyeurs_lazy(G, offline):
     assert "int16 (*__restrict__ VerTetBalTab)[2]" in s
     assert "const int *__restrict__ VerTetDegTab" in s
     assert "#define   OptCrdDegMax 32" in s
-    assert "gml_up<float4,4> OptCrd" in s
-    assert "gml_voy VerTetVoy" in s
+    assert "gml_up<float4,4,4> OptCrd = { OptCrdTab, &VerTetBalRow, OptCrdDeg };" in s
+    assert "const gml_voy<4> VerTetVoy = { &VerTetBalRow };" in s
     assert "VerCrdTab[ cnt + count.s1 ] = VerCrd;" in s
     # the degree is read before the accessors capture it
     assert s.index("VerTetDeg =  VerTetDegTab") < s.index("int OptCrdDeg = VerTetDeg;")
