@@ -67,6 +67,9 @@ def parse():
                         "batch: 512 meshes through the tile queue vs the per-mesh launch loop; "
                         "serve: the request loop on a Poisson stream; p2: the P2Quality flow "
                         "through a generated kernel")
+    p.add_argument("--degree-sort", action="store_true",
+                   help="nodesmooth: after the Hilbert numbering, put the vertices in at most "
+                        "32 tets first (GmlxDegreeSort)")
     p.add_argument("--meshes", type=int, default=512, help="batch: number of meshes")
     p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     p.add_argument("--rate", type=float, default=200.0, help="serve: requests per second")
@@ -666,7 +669,8 @@ def run_nodesmooth(args, dist):
     per-kernel device times with CUDA events over back-to-back launches."""
     import gmlib_gb300 as G
     n = args.n
-    crd, tet, ref = mesh(n)
+    dsort = 32 if args.degree_sort else 0
+    crd, tet, ref = G.cube_mesh(n, split=SPLIT, jitter=JITTER, seed=SEED, degree_sort=dsort)
     nv, nt = len(crd), len(tet)
     g = G.lib.GmlInit(dist.local)
     if not g:
@@ -749,6 +753,8 @@ def run_nodesmooth(args, dist):
                 "config": {"workload": "NodeSmoothing example flow (quality + sum, 10 x "
                                        "(scatter, gather, residual sum), quality + sum), "
                                        "%d^3-hex cube, reflected split" % n,
+                           "numbering": "Hilbert, then vertices in at most 32 tets first "
+                                        "(GmlxDegreeSort)" if dsort else "Hilbert",
                            "tets": nt, "vertices": nv, "vertex_tet_degrees": degree_summary([tet]),
                            "l2": "inputs larger than L2 (OptCrd alone is %.0f MB)" % (64e-6 * nt),
                            "step": "wall clock of the flow, host reductions included; the "

@@ -100,6 +100,7 @@ SIGNATURES = {
     "GmlxCubeSizes": (None, [_i, _ip, _ip]),
     "GmlxCubeMesh": (_i, [_i, _i, _d, ctypes.c_uint64, _p, _p, _p]),
     "GmlxHilbertRenumber": (_i, [_i, _p, _p, _i, _p, _p]),
+    "GmlxDegreeSort": (_i, [_i, _p, _p, _i, _p, _i, _p]),
 }
 
 
@@ -217,8 +218,10 @@ def as_ptr(a):
     return ctypes.c_void_p(a.ctypes.data)
 
 
-def cube_mesh(n, split=0, jitter=0.25, seed=12345, hilbert=True):
-    """Jittered n^3-hex cube split in 6 tets per hex (library generator)."""
+def cube_mesh(n, split=0, jitter=0.25, seed=12345, hilbert=True, degree_sort=0):
+    """Jittered n^3-hex cube split in 6 tets per hex (library generator),
+    Hilbert renumbered; degree_sort > 0 then puts the vertices in at most
+    that many tets first (GmlxDegreeSort)."""
     nv, nt = ctypes.c_int(), ctypes.c_int()
     lib.GmlxCubeSizes(n, ctypes.byref(nv), ctypes.byref(nt))
     crd = np.zeros((nv.value, 4), np.float32)
@@ -227,6 +230,9 @@ def cube_mesh(n, split=0, jitter=0.25, seed=12345, hilbert=True):
     lib.GmlxCubeMesh(n, split, float(jitter), int(seed), as_ptr(crd), as_ptr(tet), as_ptr(ref))
     if hilbert:
         lib.GmlxHilbertRenumber(nv.value, as_ptr(crd), as_ptr(ref), nt.value, as_ptr(tet), None)
+    if degree_sort > 0 and lib.GmlxDegreeSort(nv.value, as_ptr(crd), as_ptr(ref), nt.value,
+                                              as_ptr(tet), degree_sort, None) < 0:
+        raise RuntimeError("GmlxDegreeSort failed")
     return crd, tet, ref
 
 

@@ -632,3 +632,59 @@ int GmlxHilbertRenumber(int NmbVer, float *crd, int *ref, int NmbTet, int *tet, 
    free(nw);
    return 1;
 }
+
+/* Stable partition of the vertices by tetrahedron degree, the second half
+   of the reference's renumbering (lower degrees first, higher degrees at
+   the end of the table, Documentation/GMlib3_en.tex:401): vertices in at
+   most BalSiz tetrahedra first, then the others, each group in its previous
+   order.  The ball tables start their wide part at the first vertex above
+   BalSiz (gmlib3.c:930-937), so without this every vertex behind that one
+   goes through the wide table. */
+int GmlxDegreeSort(int NmbVer, float *crd, int *ref, int NmbTet, int *tet, int BalSiz,
+                   int *VerPrm)
+{
+   int *deg, *nw, *tmpi, i, low = 0, pos[2];
+   float *tmpf;
+
+   if(NmbVer < 1 || NmbTet < 0 || (NmbTet > 0 && !tet) || !crd || BalSiz < 1)
+      return -1;
+   deg = calloc((size_t)NmbVer, sizeof(int));
+   nw = malloc((size_t)NmbVer * sizeof(int));
+   tmpf = malloc((size_t)NmbVer * 4 * sizeof(float));
+   tmpi = malloc((size_t)NmbVer * sizeof(int));
+   if(!deg || !nw || !tmpf || !tmpi)
+   {
+      free(deg); free(nw); free(tmpf); free(tmpi);
+      return -1;
+   }
+   for(i=0;i<4*NmbTet;i++)
+   {
+      if(tet[i] < 0 || tet[i] >= NmbVer)
+      {
+         free(deg); free(nw); free(tmpf); free(tmpi);
+         return -1;
+      }
+      deg[ tet[i] ]++;
+   }
+   for(i=0;i<NmbVer;i++)
+      low += deg[i] <= BalSiz;
+   pos[0] = 0;
+   pos[1] = low;
+   for(i=0;i<NmbVer;i++)
+      nw[i] = pos[ deg[i] > BalSiz ]++;
+
+   for(i=0;i<NmbVer;i++)
+   {
+      memcpy(&tmpf[ 4 * nw[i] ], &crd[ 4*i ], 4 * sizeof(float));
+      if(ref) tmpi[ nw[i] ] = ref[i];
+   }
+   memcpy(crd, tmpf, (size_t)NmbVer * 4 * sizeof(float));
+   if(ref) memcpy(ref, tmpi, (size_t)NmbVer * sizeof(int));
+   for(i=0;i<4*NmbTet;i++)
+      tet[i] = nw[ tet[i] ];
+   if(VerPrm)
+      memcpy(VerPrm, nw, (size_t)NmbVer * sizeof(int));
+
+   free(deg); free(nw); free(tmpf); free(tmpi);
+   return low;
+}

@@ -1627,6 +1627,3 @@ float GmlEvaluateNumbering(size_t GmlIdx)
 
    return (hit + mis) ? 100 * (float)hit / (float)(hit + mis) : 0.f;
 }
-
-/* Face extraction is not part of the GB300 path (no configuration uses it);
-   the entry point exists so that existing programs link, and reports it. */

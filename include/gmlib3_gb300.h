@@ -400,6 +400,17 @@ int      GmlxCubeMesh         (int n, int split, double jitter, uint64_t seed,
 int      GmlxHilbertRenumber  (int NmbVer, float *crd, int *ref, int NmbTet, int *tet,
                                int *VerPrm);
 
+/* Stable partition of the vertices by the number of tetrahedra they belong
+   to: those in at most BalSiz tetrahedra first, then the others, each group
+   keeping its order (call it after GmlxHilbertRenumber).  This is the
+   numbering the reference's ball tables expect (low degrees first,
+   Documentation/GMlib3_en.tex:401); BalSiz is the base ball width, 32 for
+   vertex -> tetrahedron balls.  Arrays are permuted in place; VerPrm
+   (optional) receives the new index of each old vertex.  Returns the size
+   of the first group, or -1 on bad arguments (a tet index out of range). */
+int      GmlxDegreeSort       (int NmbVer, float *crd, int *ref, int NmbTet, int *tet,
+                               int BalSiz, int *VerPrm);
+
 #ifdef __cplusplus
 }
 #endif
