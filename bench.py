@@ -539,6 +539,8 @@ def run_quality(args, dist):
     if G.lib.GmlxMeshSetup(g, 1) != 1:
         raise SystemExit("GmlxMeshSetup failed")
     flush = G.lib.GmlNewVector(g, 16 << 20, 4, None, G.GmlFlt)     # 256 MB
+    if flush <= 0:
+        raise SystemExit("cannot allocate the L2 flush vector")
     one = ctypes.c_double(1.0)
     res = G.GmlxQuality()
 
