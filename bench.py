@@ -413,6 +413,53 @@ SOLVE_N = 96
 SOLVE_TOL = 1e-10
 
 
+VOP_LINES = 12 << 20       # vector lines of the vector-op timings (larger than L2)
+
+
+def vector_ops(G, dev, peak):
+    """The reference API's vector operations on 3-blocks (GmlAddVec3,
+    GmlScaleVec, GmlMultDiagMatVec with 3x3 diagonal blocks) in FP32 and
+    FP64 over VOP_LINES lines, each precision in an instance of its own:
+    device time per launch, CUDA events over 20 back-to-back launches.
+    Algorithmic bytes count the 3 (or 9) used values per line, reads and
+    writes; the stored lines are padded to 4 (or 16) values, as the
+    reference's vectors are."""
+    out = {}
+    nl = VOP_LINES
+    for fname, ft, fs in (("f32", G.GmlFlt, 4), ("f64", G.GmlDbl, 8)):
+        g = G.lib.GmlInit(dev)
+        if not g:
+            raise SystemExit("GmlInit failed")
+        G.lib.GmlxSetTiming(g, 0)
+        a, b, c, d = (G.lib.GmlNewVector(g, nl, 3, None, ft) for _ in range(4))
+        dg = G.lib.GmlNewVector(g, nl, 9, None, ft)
+        if min(a, b, c, d, dg) <= 0:
+            raise SystemExit("vector allocation failed")
+        e0, e1 = G.lib.GmlxEventCreate(), G.lib.GmlxEventCreate()
+        mul = ctypes.c_double(0.5)
+        ops = (("add3", lambda: G.lib.GmlAddVec3(g, a, b, c, d), 4 * 3 * fs),
+               ("scale", lambda: G.lib.GmlScaleVec(g, a, ctypes.byref(mul)), 2 * 3 * fs),
+               ("diag", lambda: G.lib.GmlMultDiagMatVec(g, dg, b, c), (9 + 3 + 3) * fs))
+        res = {}
+        for name, fn, per_line in ops:
+            for _ in range(3):
+                fn()
+            G.lib.GmlxSynchronize(g)
+            G.lib.GmlxEventRecord(g, e0)
+            for _ in range(20):
+                if fn() != 1:
+                    raise SystemExit("%s failed" % name)
+            G.lib.GmlxEventRecord(g, e1)
+            t = G.lib.GmlxEventElapsed(e0, e1) / 20
+            byt = per_line * float(nl)
+            res[name] = {"mean_launch_us": round(t * 1e6, 2), "algorithmic_bytes": byt,
+                         "achieved_gbs": round(byt / t / 1e9, 1),
+                         "frac": round(byt / t / 1e9 / peak, 4)}
+        G.lib.GmlStop(g)
+        out[fname] = res
+    return out
+
+
 def run_solve(args, dist):
     """Block SpMV and CG on the 3x3-block SPD system of the vertex graph of a
     96^3-hex cube (912,673 rows, 13,465,441 blocks): SpMV launch times in FP32
@@ -459,6 +506,8 @@ def run_solve(args, dist):
                       "achieved_gbs": round(byt / t / 1e9, 1), "frac": round(byt / t / 1e9 / peak, 4),
                       "gflops": round(18.0 * nnzb / t / 1e9, 1)}
 
+    vops = vector_ops(G, dist.local, peak)
+
     solves = {}
     clocks = Clocks(dist.local)
     clocks.start()
@@ -487,7 +536,8 @@ def run_solve(args, dist):
                                        "tet cube" % n, "rows": nrow, "blocks": nnzb,
                            "tol": SOLVE_TOL, "inputs": "larger than L2 (FP64 matrix %.0f MB)"
                            % (76.0 * nnzb / 1e6)},
-                "spmv": spmv, "solves": solves, "peak_gbs": peak, "peak_source": peak_src,
+                "spmv": spmv, "vector_ops": vops, "solves": solves, "peak_gbs": peak,
+                "peak_source": peak_src,
                 "clocks": clk}
         print(json.dumps(line), flush=True)
 

@@ -203,6 +203,16 @@ extern "C" int gmd_vec_add3(GmdCtx *ctx, const void *u, const void *v, const voi
    return cudaGetLastError() == cudaSuccess;
 }
 
+__device__ __forceinline__ float4 scale16(float4 a, float s)
+{
+   return make_float4(a.x * s, a.y * s, a.z * s, a.w * s);
+}
+
+__device__ __forceinline__ double2 scale16(double2 a, double s)
+{
+   return make_double2(a.x * s, a.y * s);
+}
+
 template<class T>
 __global__ void __launch_bounds__(LA_THREADS) scale_kernel(T *__restrict__ u, size_t n, T s)
 {
@@ -211,12 +221,34 @@ __global__ void __launch_bounds__(LA_THREADS) scale_kernel(T *__restrict__ u, si
       u[i] *= s;
 }
 
+/* in place, 16 bytes per access and two accesses in flight per thread */
+template<class V, class T>
+__global__ void __launch_bounds__(LA_THREADS) scale16_kernel(V *__restrict__ u, size_t n16, T s)
+{
+   const size_t nth = (size_t)gridDim.x * blockDim.x;
+   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+   for(;i + nth < n16;i+=2*nth)
+   {
+      V a = u[i], b = u[i + nth];
+      u[i] = scale16(a, s);
+      u[i + nth] = scale16(b, s);
+   }
+   if(i < n16)
+      u[i] = scale16(u[i], s);
+}
+
 extern "C" int gmd_vec_scale(GmdCtx *ctx, void *u, size_t n, int fltsiz, double s)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
    if(!ctx)
       return 0;
-   if(fltsiz == 4)
+   if(fltsiz == 4 && n % 4 == 0 && ((uintptr_t)u & 15) == 0)
+      scale16_kernel<float4, float><<<grid_for(ctx, n / 4), LA_THREADS, 0, st>>>((float4 *)u, n / 4,
+                                                                                 (float)s);
+   else if(fltsiz == 8 && n % 2 == 0 && ((uintptr_t)u & 15) == 0)
+      scale16_kernel<double2, double><<<grid_for(ctx, n / 2), LA_THREADS, 0, st>>>((double2 *)u,
+                                                                                   n / 2, s);
+   else if(fltsiz == 4)
       scale_kernel<float><<<grid_for(ctx, n), LA_THREADS, 0, st>>>((float *)u, n, (float)s);
    else
       scale_kernel<double><<<grid_for(ctx, n), LA_THREADS, 0, st>>>((double *)u, n, s);
@@ -278,6 +310,39 @@ diag_kernel(const T *__restrict__ d, int ds, const T *__restrict__ u, T *__restr
       vl[i] = (T)0;
 }
 
+/* 3x3 blocks, the common case: the block line (9 of 16 stored values) and
+   the vector lines (3 of 4) move as 16-byte pieces.  The products are summed
+   in the generic kernel's order, so the results are the same. */
+__global__ void __launch_bounds__(LA_THREADS)
+diag3_f32_kernel(const float4 *__restrict__ d, int ds4, const float4 *__restrict__ u,
+                 float4 *__restrict__ v, int nlin)
+{
+   const int l = blockIdx.x * blockDim.x + threadIdx.x;
+   if(l >= nlin)
+      return;
+   const float4 *dl = d + (size_t)l * ds4;
+   const float4 a = __ldg(dl), b = __ldg(dl + 1), c = __ldg(dl + 2), x = __ldg(u + l);
+   v[l] = make_float4(a.x * x.x + a.y * x.y + a.z * x.z,
+                      a.w * x.x + b.x * x.y + b.y * x.z,
+                      b.z * x.x + b.w * x.y + c.x * x.z, 0.f);
+}
+
+__global__ void __launch_bounds__(LA_THREADS)
+diag3_f64_kernel(const double2 *__restrict__ d, int ds2, const double2 *__restrict__ u,
+                 double2 *__restrict__ v, int nlin)
+{
+   const int l = blockIdx.x * blockDim.x + threadIdx.x;
+   if(l >= nlin)
+      return;
+   const double2 *dl = d + (size_t)l * ds2;
+   const double2 m0 = __ldg(dl), m1 = __ldg(dl + 1), m2 = __ldg(dl + 2), m3 = __ldg(dl + 3);
+   const double2 m4 = __ldg(dl + 4), x0 = __ldg(u + 2 * (size_t)l), x1 = __ldg(u + 2 * (size_t)l + 1);
+   /* block values m00 m01 | m02 m10 | m11 m12 | m20 m21 | m22 -, vector x y | z - */
+   v[2 * (size_t)l]     = make_double2(m0.x * x0.x + m0.y * x0.y + m1.x * x1.x,
+                                       m1.y * x0.x + m2.x * x0.y + m2.y * x1.x);
+   v[2 * (size_t)l + 1] = make_double2(m3.x * x0.x + m3.y * x0.y + m4.x * x1.x, 0.);
+}
+
 extern "C" int gmd_vec_diag(GmdCtx *ctx, const void *d, int ds, const void *u, void *v, int vs,
                             int b, int fltsiz, int nlin)
 {
@@ -285,6 +350,19 @@ extern "C" int gmd_vec_diag(GmdCtx *ctx, const void *d, int ds, const void *u, v
    int nb = (nlin + LA_THREADS - 1) / LA_THREADS;
    if(!ctx || b > 8)
       return 0;
+   const int aligned = !(((uintptr_t)d | (uintptr_t)u | (uintptr_t)v) & 15);
+   if(b == 3 && vs == 4 && aligned && fltsiz == 4 && ds % 4 == 0 && ds >= 12)
+   {
+      diag3_f32_kernel<<<nb, LA_THREADS, 0, st>>>((const float4 *)d, ds / 4, (const float4 *)u,
+                                                  (float4 *)v, nlin);
+      return cudaGetLastError() == cudaSuccess;
+   }
+   if(b == 3 && vs == 4 && aligned && fltsiz == 8 && ds % 2 == 0 && ds >= 10)
+   {
+      diag3_f64_kernel<<<nb, LA_THREADS, 0, st>>>((const double2 *)d, ds / 2, (const double2 *)u,
+                                                  (double2 *)v, nlin);
+      return cudaGetLastError() == cudaSuccess;
+   }
    if(fltsiz == 4)
       diag_kernel<float><<<nb, LA_THREADS, 0, st>>>((const float *)d, ds, (const float *)u,
                                                     (float *)v, vs, b, nlin);

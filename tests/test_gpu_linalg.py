@@ -98,6 +98,16 @@ def test_vector_operations(O, gpu, flt):
     z = read_vector(gpu, iz, nrow, b, flt)
     zexp = np.einsum("lij,lj->li", d.reshape(nrow, b, b).astype(np.float64), u.astype(np.float64))
     assert np.max(np.abs(z - zexp)) <= (1e-6 if flt == G.GmlFlt else 1e-14)
+    # the padding lane of each stored line stays zero
+    raw = G.get_data(gpu, G.lib.GmlxVectorData(gpu, iz), dt, (nrow, 4))
+    assert np.all(raw[:, 3] == 0)
+
+    # scaling a vector whose stored length is not a multiple of four values
+    s1 = rng.uniform(-1, 1, (nrow, 1)).astype(dt)
+    i1 = new_vector(gpu, s1, flt)
+    assert G.lib.GmlScaleVec(gpu, i1, ctypes.byref(mul)) == 1
+    got = G.get_data(gpu, G.lib.GmlxVectorData(gpu, i1), dt, nrow)       # one value per line
+    assert np.array_equal(got, s1[:, 0] * dt(-2.5))
 
     G.lib.GmlNewMeshData(gpu, G.GmlVertices, nrow)
     red = G.lib.GmlNewSolutionData(gpu, G.GmlVertices, 1, G.GmlFlt, b"red")
