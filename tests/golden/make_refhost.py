@@ -1,0 +1,355 @@
+"""Generate tests/golden/refhost_*.npz by running the reference's own host
+library (sources/gmlib3.c, unmodified) on the CPU.
+
+oracle/_ref/librefhost.so is that file compiled against an OpenCL stand-in
+header, with a host-CPU OpenCL runtime that builds the kernels the reference
+generates (and its library kernels) with g++ and runs them
+(oracle/refhost/, recipe oracle/build.py build_refhost).  This script calls
+the reference's API the way its examples do and stores what the reference
+produced:
+
+  refhost_kuhn_n5.npz, refhost_reflected_n6.npz   (inputs: kuhn_n5.npz and
+      reflected_n6.npz of this directory)
+    deg, base, high, n_base, n_high  vertex -> tet ball tables as uploaded by
+        NewBallData (gmlib3.c:743-1168), read from the arguments of the
+        generated NodeSmoothing gather kernel and of its high-degree twin;
+        `high` row 0 is left as the reference leaves it (never written)
+    edges          GmlExtractEdges (:3719-3873), (v0, v1) per edge
+    tri            GmlExtractFaces (:3880-4171), (v0, v1, v2, ref)
+    numbering      GmlEvaluateNumbering (:4409-4442)
+    mq_qal         examples/MeshQuality/compute_quality.cl through
+                   GmlCompileKernel/GmlLaunchKernel
+    mq_min         GmlReduceVector(GmlMin) of it (first reduction of a fresh
+                   instance; later calls with the same operation rebind no
+                   arguments, gmlib3.c:3098-3135)
+    red            GmlReduceVector(op) of mq_qal for op = Min..Linf, each the
+                   first reduction of a fresh instance
+    ns_qal0, ns_opt1, ns_crd1, ns_res1, ns_crd3
+                   the NodeSmoothing flow (NodeSmoothing.c:114-161): quality
+                   before smoothing, OptCrd and coordinates and residuals
+                   after one scatter+gather sweep, coordinates after three
+  refhost_c1.npz   the 32^3-hex Kuhn cube (jitter 0.25 h, seed 12345, Hilbert
+                   order): SHA-256 digests of deg, base, high (row 0 as
+                   above) and edges, plus numbering and the MeshQuality
+                   minimum
+  refhost_linsolve.npz   the LinearSolver flow (LinearSolver.c:157-340) on the
+                   7^3-hex Kuhn cube: CSR from GmlExtractEdges, block
+                   values from pseudo(), then D.x (b = 5 only), A.x,
+                   AddVec3, NormVec for 5 iterations, for the (block,
+                   precision) pairs of LINSOLVE: each iteration's norm and
+                   the final x; and `_ax`, y = A x0 from one
+                   GmlMultMatVec(mat, y, x) in a fresh instance.  In the
+                   example's loop GmlMultMatVec(mat, Xk0, Tmp) writes
+                   Xk0 = A Tmp, which GmlAddVec3 then overwrites, so the
+                   loop itself does not depend on A
+
+Usage:  python tests/golden/make_refhost.py        (needs the reference tree)
+"""
+import ctypes
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import build as OB  # noqa: E402
+from oracle import refhost as R  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+EX = os.path.join(OB.REF_ROOT, "examples")
+
+
+def body(rel):
+    with open(os.path.join(EX, rel), "rb") as f:
+        return f.read()
+
+
+def f32(b, shape):
+    return np.frombuffer(b, np.float32)[:int(np.prod(shape))].reshape(shape).copy()
+
+
+def i32(b, shape):
+    return np.frombuffer(b, np.int32)[:int(np.prod(shape))].reshape(shape).copy()
+
+
+def ball_and_smoothing(crd, tet, ref, sweeps):
+    """NodeSmoothing flow; returns the ball tables and the flow's results."""
+    nv, nt = len(crd), len(tet)
+    I = R.Instance()
+    I.parameters(64, body("NodeSmoothing/parameters.cl"))
+    v = I.mesh(R.GmlVertices, crd, ref)
+    I.mesh(R.GmlTetrahedra, tet)
+    q = I.solution(R.GmlTetrahedra, 1, R.GmlFlt, b"qal")
+    o = I.solution(R.GmlTetrahedra, 4, R.GmlFlt4, b"OptCrd")
+    r = I.solution(R.GmlVertices, 1, R.GmlFlt, b"res")
+    first = R.lib().refhost_nkernels()
+    kq = I.compile(body("NodeSmoothing/quality.cl"), b"quality", R.GmlTetrahedra,
+                   [(v, R.GmlReadMode), (q, R.GmlWriteMode)])
+    ks = I.compile(body("NodeSmoothing/scatter.cl"), b"scatter", R.GmlTetrahedra,
+                   [(v, R.GmlReadMode), (o, R.GmlWriteMode)])
+    kg = I.compile(body("NodeSmoothing/gather.cl"), b"gather", R.GmlVertices,
+                   [(r, R.GmlWriteMode), (o, R.GmlReadMode | R.GmlVoyeurs),
+                    (v, R.GmlReadMode | R.GmlWriteMode)])
+    objs = [k for k in R.kernel_objects("gather") if k >= first]
+    kobj = [k for k in R.kernel_objects("quality") if k >= first][0]
+    sobj = [k for k in R.kernel_objects("scatter") if k >= first][0]
+    out = {}
+    I.launch(kq)
+    out["ns_qal0"] = f32(R.kernel_buffers(kobj)["qalTab"], (nt,))
+    for s in range(1, sweeps + 1):
+        I.launch(ks)
+        I.launch(kg)
+        if s == 1:
+            out["ns_opt1"] = f32(R.kernel_buffers(sobj)["OptCrdTab"], (nt, 4, 4))
+            b = R.kernel_buffers(objs[0])
+            out["ns_crd1"] = f32(b["VerCrdTab"], (nv, 4))
+            out["ns_res1"] = f32(b["resTab"], (nv,))
+    out["ns_crd3"] = f32(R.kernel_buffers(objs[0])["VerCrdTab"], (nv, 4))
+    ok, n, w, N, W = I.link_info(R.GmlVertices, R.GmlTetrahedra)
+    assert ok == 1
+    b0 = R.kernel_buffers(objs[0])
+    out["deg"] = i32(b0["VerTetDegTab"], (nv,))
+    out["base"] = i32(b0["VerTetBalTab"], (n, w))
+    out["n_base"] = n
+    out["n_high"] = N
+    if N:
+        out["high"] = i32(R.kernel_buffers(objs[1])["VerTetBalTab"], (N, W))
+    else:
+        out["high"] = np.zeros((0, 64), np.int32)
+    I.stop()
+    return out
+
+
+def topology(crd, tet, ref):
+    I = R.Instance()
+    I.mesh(R.GmlVertices, crd, ref)
+    I.mesh(R.GmlTetrahedra, tet)
+    out = {}
+    ne = I.L.GmlExtractEdges(I.g)
+    n, e = I.mesh_info(R.GmlEdges)
+    assert ne == n
+    out["edges"] = I.get_lines(e, n, "ii")[:, :2].astype(np.int32)
+    out["numbering"] = np.float32(I.L.GmlEvaluateNumbering(I.g))
+    nf = I.L.GmlExtractFaces(I.g)
+    n, f = I.mesh_info(R.GmlTriangles)
+    assert nf == n
+    out["tri"] = I.get_lines(f, n, "iii").astype(np.int32)
+    I.stop()
+    return out
+
+
+def mesh_quality(crd, tet, ref, op=R.GmlMin):
+    """MeshQuality flow (MeshQuality.c:94-127): the compute_quality body, then
+    one reduction, the first of a fresh instance."""
+    I = R.Instance()
+    I.parameters(64, body("MeshQuality/parameters.cl"))
+    v = I.mesh(R.GmlVertices, crd, ref)
+    I.mesh(R.GmlTetrahedra, tet)
+    q = I.solution(R.GmlTetrahedra, 1, R.GmlFlt, b"qal")
+    first = R.lib().refhost_nkernels()
+    k = I.compile(body("MeshQuality/compute_quality.cl"), b"quality", R.GmlTetrahedra,
+                  [(v, R.GmlReadMode), (q, R.GmlWriteMode)])
+    I.launch(k)
+    kobj = [x for x in R.kernel_objects("quality") if x >= first][0]
+    qal = f32(R.kernel_buffers(kobj)["qalTab"], (len(tet),))
+    red = I.reduce(q, op)
+    I.stop()
+    return qal, red
+
+
+def make_case(name, src):
+    g = dict(np.load(os.path.join(OUT, src)))
+    crd, tet, ref = g["crd"], g["tet"], g["ref"]
+    out = ball_and_smoothing(crd, tet, ref, 3)
+    out.update(topology(crd, tet, ref))
+    out["mq_qal"], out["mq_min"] = mesh_quality(crd, tet, ref)
+    out["red"] = np.array([mesh_quality(crd, tet, ref, op)[1] for op in range(7)])
+    np.savez_compressed(os.path.join(OUT, name), **out)
+    print(name, {k: getattr(v, "shape", v) for k, v in out.items()})
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def make_c1():
+    import gmlib_gb300 as G
+    crd, tet, ref = G.cube_mesh(32, split=0, jitter=0.25, seed=12345)
+    out = ball_and_smoothing(crd, tet, ref, 1)
+    top = topology(crd, tet, ref)
+    qal, mn = mesh_quality(crd, tet, ref)
+    res = dict(deg=digest(out["deg"]), base=digest(out["base"]), high=digest(out["high"]),
+               edges=digest(top["edges"]), n_base=out["n_base"], n_high=out["n_high"],
+               n_edges=len(top["edges"]), n_tri=len(top["tri"]), tri=digest(top["tri"]),
+               numbering=top["numbering"], mq_min=mn, mq_argmin=int(np.argmin(qal)),
+               mesh=digest(crd) + digest(tet))
+    np.savez_compressed(os.path.join(OUT, "refhost_c1.npz"), **res)
+    print("refhost_c1.npz", res)
+
+
+def csr_from_edges(nv, edges):
+    """The LinearSolver example's CSR (LinearSolver.c:157-234): per vertex, its
+    edge partners in edge order; the diagonal lives in a separate vector."""
+    deg = np.zeros(nv + 1, np.int64)
+    for j, k in edges:
+        deg[j] += 1
+        deg[k] += 1
+    lin = np.zeros(nv + 1, np.int32)
+    lin[1:] = np.cumsum(deg[:nv])
+    fill = np.zeros(nv, np.int64)
+    col = np.zeros(lin[-1], np.int32)
+    for j, k in edges:
+        col[lin[j] + fill[j]] = k
+        fill[j] += 1
+        col[lin[k] + fill[k]] = j
+        fill[k] += 1
+    return lin, col
+
+
+def pseudo(shape, salt):
+    """Deterministic values in [-1, 1) (a 64-bit LCG step of the index), so
+    that tests rebuild the LinearSolver inputs without storing them."""
+    n = int(np.prod(shape))
+    k = (np.arange(n, dtype=np.uint64) + np.uint64(salt)) * np.uint64(6364136223846793005)
+    k = (k + np.uint64(1442695040888963407)) >> np.uint64(40)
+    return (k.astype(np.float64) / 8388608.0 - 1.0).reshape(shape)
+
+
+def linsolve_inputs(nv, nnz, b, dbl):
+    """Block values of the LinearSolver flow: off-diagonal and diagonal blocks
+    small enough that x <- D x + A x + rhs contracts, x0 and rhs in [-1, 1)."""
+    vals = 0.01 * pseudo((nnz, b * b), 11 * b + dbl)
+    diag = 0.01 * pseudo((nv, b * b), 13 * b + dbl)
+    x0 = pseudo((nv, b), 17 * b + dbl)
+    rhs = pseudo((nv, b), 19 * b + dbl)
+    if not dbl:
+        vals, diag, x0, rhs = (a.astype(np.float32) for a in (vals, diag, x0, rhs))
+    return vals, diag, x0, rhs
+
+
+# (block size, FP64, diagonal product): the reference's GmlMultDiagMatVec
+# runs the diagonal vector's own kernel, built with BLKSIZ = b*b
+# (gmlib3.c:3626, 1549-1553), whose #else branch is the 5x5 product on
+# double-width lines (multdiagmatvec.cl:44-75); it is right for b = 5 only
+# and reads and writes past its vectors otherwise, so the b = 4 flows leave
+# it out (x1 then stays x0).  b = 7 has no matrix kernels at all
+# (multmatvec.cl:1645-1663 defines only the block product), so GmlNewMatrix
+# cannot create its slice kernels and the flow cannot run.
+LINSOLVE = ((4, 0, 0), (4, 1, 0), (5, 0, 1), (5, 1, 1))
+
+
+def linsolve_run(mesh, lin, col, b, dbl, use_diag, vals, diag, x0, rhs, iters):
+    crd, tet, ref = mesh
+    nv = len(crd)
+    I = R.Instance()
+    L = I.L
+    # the mesh, as the example imports it: the norm's "reduction" field is a
+    # vertex solution and takes its line count from the vertices
+    I.mesh(R.GmlVertices, crd, ref)
+    I.mesh(R.GmlTetrahedra, tet)
+    fty = R.GmlDbl if dbl else R.GmlFlt
+    npt = np.float64 if dbl else np.float32
+    first = R.lib().refhost_nkernels()
+    A = np.ascontiguousarray(vals, npt)
+    mat = L.GmlNewMatrix(I.g, nv, len(col), b, R._p(A), R._p(col), R._p(lin), fty)
+    assert mat > 0
+    D = np.ascontiguousarray(diag, npt)
+    dia = L.GmlNewVector(I.g, nv, b * b, R._p(D), fty)
+    X = np.ascontiguousarray(x0, npt)
+    xk0 = L.GmlNewVector(I.g, nv, b, R._p(X), fty)
+    xk1 = L.GmlNewVector(I.g, nv, b, R._p(X), fty)
+    tmp = L.GmlNewVector(I.g, nv, b, R._p(X), fty)
+    Bv = np.ascontiguousarray(rhs, npt)
+    rhv = L.GmlNewVector(I.g, nv, b, R._p(Bv), fty)
+    red = I.solution(R.GmlVertices, 1, R.GmlFlt, b"reduction")
+    assert min(dia, xk0, xk1, tmp, rhv) > 0
+    norms = []
+    for _ in range(iters):
+        if use_diag:
+            assert L.GmlMultDiagMatVec(I.g, dia, xk0, xk1) == 1
+        assert L.GmlMultMatVec(I.g, mat, xk0, tmp) == 1
+        assert L.GmlAddVec3(I.g, rhv, tmp, xk1, xk0) == 1
+        nrm = ctypes.c_double()
+        assert L.GmlNormVec(I.g, xk0, red, ctypes.byref(nrm)) == 1
+        norms.append(nrm.value)
+    # GmlNewVector builds kernels per vector; GmlAddVec3 runs the first
+    # vector's (rhs here), the only AddVec object with bound arguments
+    add = [k for k in R.kernel_objects("AddVec") if k >= first and "Y" in R.kernel_buffers(k)][0]
+    width = 4 if b <= 4 else 8
+    x = np.frombuffer(R.kernel_buffers(add)["Y"], npt)[:nv * width].reshape(nv, width)[:, :b].copy()
+    I.stop()
+    return np.array(norms), x
+
+
+def spmv_run(mesh, lin, col, b, dbl, vals, x0):
+    """One GmlMultMatVec(mat, y, x) as the first call of a fresh instance:
+    the kernel takes (degrees, columns, blocks, B, X) and the library binds
+    B = its first vector, X = its second (gmlib3.c:3383-3389), so y = A x."""
+    crd, tet, ref = mesh
+    nv = len(crd)
+    I = R.Instance()
+    L = I.L
+    I.mesh(R.GmlVertices, crd, ref)
+    fty = R.GmlDbl if dbl else R.GmlFlt
+    npt = np.float64 if dbl else np.float32
+    first = R.lib().refhost_nkernels()
+    A = np.ascontiguousarray(vals, npt)
+    mat = L.GmlNewMatrix(I.g, nv, len(col), b, R._p(A), R._p(col), R._p(lin), fty)
+    X = np.ascontiguousarray(x0, npt)
+    Z = np.zeros_like(X)
+    y = L.GmlNewVector(I.g, nv, b, R._p(Z), fty)
+    x = L.GmlNewVector(I.g, nv, b, R._p(X), fty)
+    assert min(mat, y, x) > 0 and L.GmlMultMatVec(I.g, mat, y, x) == 1
+    k = [k for k in R.kernel_objects("MulMatVecSlc16") if k >= first][0]
+    width = 4 if b <= 4 else 8
+    ax = np.frombuffer(R.kernel_buffers(k)["B"], npt)[:nv * width].reshape(nv, width)[:, :b].copy()
+    I.stop()
+    return ax
+
+
+def linsolve_mesh():
+    import gmlib_gb300 as G
+    return G.cube_mesh(7, split=0, jitter=0.1, seed=99)
+
+
+def make_linsolve():
+    crd, tet, ref = linsolve_mesh()
+    top = topology(crd, tet, ref)
+    nv = len(crd)
+    lin, col = csr_from_edges(nv, top["edges"])
+    out = dict(mesh=digest(crd) + digest(tet), edges=top["edges"], lin=lin, col=col)
+    for b, dbl, use_diag in LINSOLVE:
+        vals, diag, x0, rhs = linsolve_inputs(nv, len(col), b, dbl)
+        norms, x = linsolve_run((crd, tet, ref), lin, col, b, dbl, use_diag, vals, diag, x0, rhs, 5)
+        tag = "b%d_%s" % (b, "f64" if dbl else "f32")
+        ax = spmv_run((crd, tet, ref), lin, col, b, dbl, vals, x0)
+        out.update({tag + "_norms": norms, tag + "_x": x, tag + "_ax": ax})
+        print(tag, norms)
+    np.savez_compressed(os.path.join(OUT, "refhost_linsolve.npz"), **out)
+
+
+CASES = {
+    "kuhn_n5": lambda: make_case("refhost_kuhn_n5.npz", "kuhn_n5.npz"),
+    "reflected_n6": lambda: make_case("refhost_reflected_n6.npz", "reflected_n6.npz"),
+    "linsolve": make_linsolve,
+    "c1": make_c1,
+}
+
+if __name__ == "__main__":
+    if R.lib() is None:
+        sys.exit("the reference tree is needed to run the reference host library")
+    if len(sys.argv) > 1:
+        CASES[sys.argv[1]]()
+    else:
+        # one process per case: with a vertex degree above the base width the
+        # reference writes that vertex's whole ball into its base-table row
+        # (gmlib3.c:1126-1129), past the end of the host mirror, which can
+        # corrupt the process heap; a fresh process keeps that out of the other
+        # cases, and every fixture is read before the process exits
+        import subprocess
+        for c in CASES:
+            subprocess.run([sys.executable, os.path.abspath(__file__), c], check=False)
+            print("case", c, "done")
