@@ -1,8 +1,9 @@
 /*
  * gml_codegen.c -- CUDA C++ generation for GmlCompileKernel.
  *
- * Input: the argument table built by GmlCompileKernel (same construction as
- * the reference, sources/gmlib3.c:2292-2499) and the user's OpenCL-C body.
+ * Input: the argument plan built by GmlCompileKernel (link tables, degree
+ * tables, datatypes and reference arrays in the contract's order) and the
+ * user's OpenCL-C body.
  * Output: one CUDA kernel source with the reference's naming contract, so the
  * body compiles unchanged:
  *
@@ -100,12 +101,95 @@ static int ensure_row(Out *o, const GmlArgSct *ArgTab, int NmbArg, int li, int *
    return V;
 }
 
+/* ------------------------------------------------------------------------- */
+/* Eager reads: the text of the reference's read prologue (sources/gmlib3.c:  */
+/* 2755-2885), which bodies needing real arrays compile against.  Item j of   */
+/* a datatype is read for every gather slot k of its link: the slot's index   */
+/* is link component k (vector k/16 of the line, lane k%16), guarded by the   */
+/* degree (counted uplinks) or by the component itself (neighbour links),    */
+/* and shifted right by 4 for ball entries, whose low bits are the voyeur.   */
+/* ------------------------------------------------------------------------- */
+
+/* buf = "[v]" when on, else "" */
+static const char *sub(char *buf, size_t n, int on, int v)
+{
+   if(on)
+      snprintf(buf, n, "[%d]", v);
+   else
+      buf[0] = 0;
+   return buf;
+}
+
+/* where line `cnt` of the kernel finds slot k of its link */
+static void slot_index(char *buf, size_t n, const GmlArgSct *a, const GmlArgSct *lnk, int k)
+{
+   char vec[16];
+   if(!lnk)
+      snprintf(buf, n, "%s", a->LnkDir == 1 ? "cnt" : "cnt + count.s1");
+   else if(lnk->ItmLen > 1)
+      snprintf(buf, n, "%s%s.s%c", lnk->nam, sub(vec, sizeof vec, lnk->NmbItm > 1, k / 16),
+               HexDig[ k & 15 ]);
+   else
+      snprintf(buf, n, "%s%s", lnk->nam, sub(vec, sizeof vec, lnk->NmbItm > 1, k / 16));
+}
+
+static void emit_eager_item(Out *o, const GmlArgSct *a, const GmlArgSct *lnk,
+                            const GmlArgSct *cpt, int j)
+{
+   const int slots = (lnk && lnk->NmbItm * lnk->ItmLen > 1) ? lnk->NmbItm * lnk->ItmLen : 1;
+   const int nul = cpt || (lnk && lnk->LnkDir == 0);
+   char item[32], idx[300];
+
+   sub(item, sizeof item, a->NmbItm > 1, j);
+   if(cpt)
+      emit(o, "   %sDeg = %s;\n", a->nam, cpt->nam);
+   if(nul)
+      emit(o, "   %sNul = gml_zero<%s>();\n", a->nam, GmlOclTypStr[ a->ItmTyp ]);
+
+   if(a->FlgTab & GmlVoyeurs)
+   {
+      /* a ball row: load it, split off the voyeurs, keep the entities */
+      if(lnk)
+         snprintf(idx, sizeof idx, "%s", lnk->nam);
+      else
+         slot_index(idx, sizeof idx, a, NULL, 0);
+      emit(o, "   %s%s = %sTab[ %s ]%s;\n", a->nam, item, a->nam, idx, item);
+      for(int l=0;l<a->ItmLen;l++)
+         emit(o, "   %s[%d] = %s%s.s%c & 7;\n", a->VoyNam, j * a->ItmLen + l, a->nam, item, HexDig[l]);
+      emit(o, "   %s%s = %s%s >> 4;\n", a->nam, item, a->nam, item);
+      return;
+   }
+
+   for(int k=0;k<slots;k++)
+   {
+      char slot[32], pre[300] = "", post[300] = "";
+
+      slot_index(idx, sizeof idx, a, lnk, k);
+      if(cpt)
+      {
+         snprintf(pre, sizeof pre, "(%sDeg >= %d) ?", a->nam, k + 1);
+         snprintf(post, sizeof post, ": %sNul", a->nam);
+      }
+      else if(lnk && lnk->LnkDir == 0)
+      {
+         char lane[16] = "";
+         if(lnk->ItmLen > 1)
+            snprintf(lane, sizeof lane, ".s%c", HexDig[ k & 15 ]);
+         snprintf(pre, sizeof pre, "%s%s ?", lnk->nam, lane);
+         snprintf(post, sizeof post, ": %sNul", a->nam);
+      }
+      emit(o, "   %s%s%s = %s %sTab[ %s ]%s %s %s;\n",
+           a->nam, sub(slot, sizeof slot, slots > 1, k), item, pre, a->nam, idx, item,
+           a->LnkDir == 1 ? ">> 4" : "", post);
+   }
+}
+
 int gml_generate(char **res, const char *PrcNam, int MshTyp, int NmbArg,
                  const GmlArgSct *ArgTab, const char *KrnSrc, const char *UsrTlk,
                  const char *ParSrc, int lazy)
 {
    Out o;
-   int i, j, k, l, V;
+   int i, j, V;
    char *tmp;
 
    o.cap = 16384;
@@ -210,7 +294,6 @@ int gml_generate(char **res, const char *PrcNam, int MshTyp, int NmbArg,
       const GmlArgSct *a = &ArgTab[i];
       const GmlArgSct *lnk = a->LnkIdx != -1 ? &ArgTab[ a->LnkIdx ] : NULL;
       const GmlArgSct *cpt = a->CntIdx != -1 ? &ArgTab[ a->CntIdx ] : NULL;
-      int siz;
 
       if(!(a->FlgTab & GmlReadMode) || (a->FlgTab & GmlManual))
          continue;
@@ -219,69 +302,8 @@ int gml_generate(char **res, const char *PrcNam, int MshTyp, int NmbArg,
       if(lazy && a->LnkDir == 1 && a->NmbItm > 1)
          continue;
 
-      siz = (lnk && lnk->NmbItm * lnk->ItmLen > 1) ? lnk->NmbItm * lnk->ItmLen : 1;
-
       for(j=0;j<a->NmbItm;j++)
-      {
-         char ArgTd1[32] = "", LnkNam[256], CptNam[256] = "";
-
-         if(cpt)
-         {
-            snprintf(CptNam, sizeof(CptNam), "%sDeg", a->nam);
-            emit(&o, "   %s = %s;\n", CptNam, cpt->nam);
-            emit(&o, "   %sNul = gml_zero<%s>();\n", a->nam, GmlOclTypStr[ a->ItmTyp ]);
-         }
-         else if(lnk && lnk->LnkDir == 0)
-            emit(&o, "   %sNul = gml_zero<%s>();\n", a->nam, GmlOclTypStr[ a->ItmTyp ]);
-
-         if(a->NmbItm > 1)
-            snprintf(ArgTd1, sizeof(ArgTd1), "[%d]", j);
-
-         if(lnk)
-            snprintf(LnkNam, sizeof(LnkNam), "%s", lnk->nam);
-         else if(a->LnkDir == 1)
-            snprintf(LnkNam, sizeof(LnkNam), "cnt");
-         else
-            snprintf(LnkNam, sizeof(LnkNam), "cnt + count.s1");
-
-         if(a->FlgTab & GmlVoyeurs)
-         {
-            emit(&o, "   %s%s = %sTab[ %s ]%s;\n", a->nam, ArgTd1, a->nam, LnkNam, ArgTd1);
-            for(l=0;l<a->ItmLen;l++)
-               emit(&o, "   %s[%d] = %s%s.s%c & 7;\n", a->VoyNam, j * a->ItmLen + l,
-                    a->nam, ArgTd1, HexDig[l]);
-            emit(&o, "   %s%s = %s%s >> 4;\n", a->nam, ArgTd1, a->nam, ArgTd1);
-            continue;
-         }
-
-         for(k=0;k<siz;k++)
-         {
-            char ArgTd2[32] = "", LnkTd1[32] = "", LnkTd2[16] = "", DegTst[300] = "", DegNul[300] = "";
-            const char *BalSft = a->LnkDir == 1 ? ">> 4" : "";
-
-            if(siz > 1)
-               snprintf(ArgTd2, sizeof(ArgTd2), "[%d]", k);
-            if(lnk && lnk->NmbItm > 1)
-               snprintf(LnkTd1, sizeof(LnkTd1), "[%d]", k / 16);
-            if(lnk && lnk->ItmLen > 1)
-               snprintf(LnkTd2, sizeof(LnkTd2), ".s%c", HexDig[ k & 15 ]);
-
-            if(cpt)
-            {
-               snprintf(DegTst, sizeof(DegTst), "(%s >= %d) ?", CptNam, k + 1);
-               snprintf(DegNul, sizeof(DegNul), ": %sNul", a->nam);
-            }
-            else if(lnk && lnk->LnkDir == 0)
-            {
-               snprintf(DegTst, sizeof(DegTst), "%s%s ?", lnk->nam, LnkTd2);
-               snprintf(DegNul, sizeof(DegNul), ": %sNul", a->nam);
-            }
-
-            emit(&o, "   %s%s%s = %s %sTab[ %s%s%s ]%s %s %s;\n",
-                 a->nam, ArgTd2, ArgTd1, DegTst, a->nam, LnkNam, LnkTd1, LnkTd2, ArgTd1,
-                 BalSft, DegNul);
-         }
-      }
+         emit_eager_item(&o, a, lnk, cpt, j);
       emit(&o, "\n");
    }
 

@@ -308,151 +308,116 @@ int GmlCheckFP64(size_t GmlIdx)
 /* datatypes                                                                  */
 /* ========================================================================= */
 
-void *GmlNewParameters(size_t GmlIdx, int siz, char *src)
+/* The shape of a datatype: what kind of data it is, which entities its lines
+   follow, and how a line is made (cnt items of the OpenCL type `typ`, `len`
+   scalars each, `siz` bytes each).  Every creator below describes its
+   datatype with one of these and hands it to new_datatype(). */
+typedef struct
 {
-   int idx;
-   GmlDatSct *dat;
-   GETGMLPTR(gml, GmlIdx);
+   int         kind, msh, lnk, typ, cnt, len, siz, lines;
+   const char  *name;
+   char        *src;
+}GmlShape;
 
-   if(!(idx = gml_new_data_idx(gml)))
-      return NULL;
+/* Take a free slot, give it the shape, allocate the device buffer and the
+   host mirror.  `what` names the datatype in the debug trace, which opens a
+   new block unless `more` (a second datatype of the same call). */
+static int new_datatype(GmlSct *gml, const GmlShape *shp, const char *what, int more)
+{
+   const int idx = gml_new_data_idx(gml);
+   GmlDatSct *d;
 
-   dat = &gml->dat[ idx ];
-   dat->AloTyp = GmlArgDat;
-   dat->MemAcs = GmlInout;
-   dat->NmbItm = 1;
-   dat->ItmSiz = siz;
-   dat->NmbLin = 1;
-   dat->LinSiz = siz;
-   dat->MemSiz = (size_t)siz;
-   dat->nam    = "GmlParSct";
-   dat->src    = src;
+   if(!idx)
+      return 0;
 
-   if(!gml_alloc_data(gml, dat))
+   d = &gml->dat[ idx ];
+   d->AloTyp = shp->kind;
+   d->MshTyp = shp->msh;
+   d->LnkTyp = shp->lnk;
+   d->MemAcs = GmlInout;
+   d->ItmTyp = shp->typ;
+   d->NmbItm = shp->cnt;
+   d->ItmLen = shp->len;
+   d->ItmSiz = shp->siz;
+   d->NmbLin = shp->lines;
+   d->LinSiz = shp->cnt * shp->siz;
+   d->MemSiz = (size_t)shp->lines * (size_t)d->LinSiz;
+   d->nam    = shp->name;
+   d->src    = shp->src;
+
+   if(!gml_alloc_data(gml, d))
    {
-      dat->use = 0;
-      return NULL;
+      d->use = 0;
+      return 0;
    }
-
-   gml->ParIdx = idx;
 
    if(gml->DbgFlg)
    {
-      puts(sep);
-      printf("Allocated a parameters data: index=%2d, size=%zu bytes\n", idx, dat->MemSiz);
+      if(!more)
+         puts(sep);
+      printf("Allocated %s: index=%2d, size=%zu bytes\n", what, idx, d->MemSiz);
    }
+   return idx;
+}
 
-   return dat->CpuMem;
+/* the shape of a mesh datatype's lines: one OpenCL vector wide enough for
+   an element's nodes (vertices: float4 coordinates) */
+static GmlShape element_shape(int MshTyp, int NmbLin)
+{
+   const int typ = GmlMshItmTyp[ MshTyp ];
+   return (GmlShape){ GmlEleDat, MshTyp, 0, typ, 1, GmlTypVecSiz[ typ ], GmlOclTypSiz[ typ ],
+                      NmbLin, GmlMshTypStr[ MshTyp ], NULL };
+}
+
+void *GmlNewParameters(size_t GmlIdx, int siz, char *src)
+{
+   GETGMLPTR(gml, GmlIdx);
+   const GmlShape shp = { GmlArgDat, 0, 0, 0, 1, 0, siz, 1, "GmlParSct", src };
+   const int idx = siz >= 0 ? new_datatype(gml, &shp, "a parameters data", 0) : 0;
+
+   if(!idx)
+      return NULL;
+   gml->ParIdx = idx;
+   return gml->dat[ idx ].CpuMem;
 }
 
 int GmlNewMeshData(size_t GmlIdx, int MshTyp, int NmbLin)
 {
-   int EleIdx, RefIdx;
-   GmlDatSct *EleDat, *RefDat;
    GETGMLPTR(gml, GmlIdx);
+   int EleIdx, RefIdx;
 
    if(MshTyp < 0 || MshTyp >= GmlMaxEleTyp || NmbLin < 0)
       return 0;
 
-   if(!(EleIdx = gml_new_data_idx(gml)))
-      return 0;
-
-   EleDat = &gml->dat[ EleIdx ];
-   EleDat->AloTyp = GmlEleDat;
-   EleDat->MshTyp = MshTyp;
-   EleDat->MemAcs = GmlInout;
-   EleDat->ItmTyp = GmlMshItmTyp[ MshTyp ];
-   EleDat->NmbItm = 1;
-   EleDat->ItmSiz = GmlOclTypSiz[ EleDat->ItmTyp ];
-   EleDat->ItmLen = GmlTypVecSiz[ EleDat->ItmTyp ];
-   EleDat->NmbLin = NmbLin;
-   EleDat->LinSiz = EleDat->ItmSiz;
-   EleDat->MemSiz = (size_t)NmbLin * (size_t)EleDat->LinSiz;
-   EleDat->nam    = GmlMshTypStr[ MshTyp ];
-
-   if(!gml_alloc_data(gml, EleDat))
+   /* the element (or coordinate) lines, then one int reference per line */
    {
-      EleDat->use = 0;
-      return 0;
-   }
-
-   if(!(RefIdx = gml_new_data_idx(gml)))
-      return 0;
-
-   RefDat = &gml->dat[ RefIdx ];
-   RefDat->AloTyp = GmlRefDat;
-   RefDat->MshTyp = MshTyp;
-   RefDat->MemAcs = GmlInout;
-   RefDat->ItmTyp = GmlInt;
-   RefDat->NmbItm = 1;
-   RefDat->ItmSiz = 4;
-   RefDat->ItmLen = 0;
-   RefDat->NmbLin = NmbLin;
-   RefDat->LinSiz = 4;
-   RefDat->MemSiz = (size_t)NmbLin * 4;
-   RefDat->nam    = GmlMshRefStr[ MshTyp ];
-
-   if(!gml_alloc_data(gml, RefDat))
-   {
-      RefDat->use = 0;
-      return 0;
+      const GmlShape ele = element_shape(MshTyp, NmbLin);
+      const GmlShape ref = { GmlRefDat, MshTyp, 0, GmlInt, 1, 0, 4, NmbLin,
+                             GmlMshRefStr[ MshTyp ], NULL };
+      if(!(EleIdx = new_datatype(gml, &ele, "mesh data", 0))
+      || !(RefIdx = new_datatype(gml, &ref, "ref  data", 1)))
+         return 0;
    }
 
    gml->NmbEle[ MshTyp ] = NmbLin;
    gml->TypIdx[ MshTyp ] = EleIdx;
-   gml->LnkMat[ MshTyp ][ GmlVertices ] = EleIdx;
    gml->RefIdx[ MshTyp ] = RefIdx;
-
-   if(gml->DbgFlg)
-   {
-      puts(sep);
-      printf("Allocated mesh data: index=%2d, size=%zu bytes\n", EleIdx, EleDat->MemSiz);
-      printf("Allocated ref  data: index=%2d, size=%zu bytes\n", RefIdx, RefDat->MemSiz);
-   }
-
+   gml->LnkMat[ MshTyp ][ GmlVertices ] = EleIdx;    /* the element table is the downlink */
    return EleIdx;
 }
 
 int GmlNewSolutionData(size_t GmlIdx, int MshTyp, int NmbDat, int ItmTyp, char *nam)
 {
-   int idx;
-   GmlDatSct *dat;
    GETGMLPTR(gml, GmlIdx);
 
-   if(MshTyp < 0 || MshTyp >= GmlMaxEleTyp)
-      return 0;
-   if(ItmTyp < GmlInt || ItmTyp >= GmlMaxOclTyp || NmbDat < 1)
+   if(MshTyp < 0 || MshTyp >= GmlMaxEleTyp || ItmTyp < GmlInt || ItmTyp >= GmlMaxOclTyp || NmbDat < 1)
       return 0;
 
-   if(!(idx = gml_new_data_idx(gml)))
-      return 0;
-
-   dat = &gml->dat[ idx ];
-   dat->AloTyp = GmlRawDat;
-   dat->MshTyp = MshTyp;
-   dat->MemAcs = GmlInout;
-   dat->ItmTyp = ItmTyp;
-   dat->NmbItm = NmbDat;
-   dat->ItmSiz = GmlOclTypSiz[ ItmTyp ];
-   dat->ItmLen = GmlTypVecSiz[ ItmTyp ];
-   dat->NmbLin = gml->NmbEle[ MshTyp ];
-   dat->LinSiz = dat->NmbItm * dat->ItmSiz;
-   dat->MemSiz = (size_t)dat->NmbLin * (size_t)dat->LinSiz;
-   dat->nam    = nam;
-
-   if(!gml_alloc_data(gml, dat))
    {
-      dat->use = 0;
-      return 0;
+      const GmlShape shp = { GmlRawDat, MshTyp, 0, ItmTyp, NmbDat, GmlTypVecSiz[ ItmTyp ],
+                             GmlOclTypSiz[ ItmTyp ], gml->NmbEle[ MshTyp ], nam, NULL };
+      return new_datatype(gml, &shp, "solutions data", 0);
    }
-
-   if(gml->DbgFlg)
-   {
-      puts(sep);
-      printf("Allocated solutions data: index=%2d, size=%zu bytes\n", idx, dat->MemSiz);
-   }
-
-   return idx;
 }
 
 /* User link table (reference :693-736).  A line holds NmbDat entity indices
@@ -461,48 +426,20 @@ int GmlNewSolutionData(size_t GmlIdx, int MshTyp, int NmbDat, int ItmTyp, char *
    GmlSetNeighbours passes). */
 int GmlNewLinkData(size_t GmlIdx, int MshTyp, int LnkTyp, int NmbDat, char *nam)
 {
-   int idx, VecCnt, VecSiz, ItmTyp;
-   GmlDatSct *dat;
    GETGMLPTR(gml, GmlIdx);
+   int cnt, width, typ, idx;
 
-   if(MshTyp < 0 || MshTyp >= GmlMaxEleTyp || LnkTyp < 0 || LnkTyp >= GmlMaxEleTyp)
-      return 0;
-   if(NmbDat < 1)
-      return 0;
-
-   if(!(idx = gml_new_data_idx(gml)))
+   if(MshTyp < 0 || MshTyp >= GmlMaxEleTyp || LnkTyp < 0 || LnkTyp >= GmlMaxEleTyp || NmbDat < 1)
       return 0;
 
-   gml_get_cnt_vec(NmbDat, &VecCnt, &VecSiz, &ItmTyp);
-
-   dat = &gml->dat[ idx ];
-   dat->AloTyp = GmlLnkDat;
-   dat->MshTyp = MshTyp;
-   dat->LnkTyp = LnkTyp;
-   dat->MemAcs = GmlInout;
-   dat->ItmTyp = ItmTyp;
-   dat->NmbItm = VecCnt;
-   dat->ItmSiz = GmlOclTypSiz[ ItmTyp ];
-   dat->ItmLen = NmbDat;
-   dat->NmbLin = gml->NmbEle[ MshTyp ];
-   dat->LinSiz = VecCnt * dat->ItmSiz;
-   dat->MemSiz = (size_t)dat->NmbLin * (size_t)dat->LinSiz;
-   dat->nam    = nam;
-
-   if(!gml_alloc_data(gml, dat))
+   gml_get_cnt_vec(NmbDat, &cnt, &width, &typ);
    {
-      dat->use = 0;
-      return 0;
+      const GmlShape shp = { GmlLnkDat, MshTyp, LnkTyp, typ, cnt, NmbDat, GmlOclTypSiz[ typ ],
+                             gml->NmbEle[ MshTyp ], nam, NULL };
+      if(!(idx = new_datatype(gml, &shp, "link data", 0)))
+         return 0;
    }
-
    gml->LnkMat[ MshTyp ][ LnkTyp ] = idx;
-
-   if(gml->DbgFlg)
-   {
-      puts(sep);
-      printf("Allocated link data: index=%2d, size=%zu bytes\n", idx, dat->MemSiz);
-   }
-
    return idx;
 }
 
@@ -1233,290 +1170,260 @@ static int build_kernel(GmlSct *gml, char *KrnSrc, char *PrcNam, int MshTyp,
    return idx;
 }
 
+/* ------------------------------------------------------------------------- */
+/* Kernel argument planning.                                                  */
+/*                                                                           */
+/* The generated kernel's parameter list is part of the naming contract      */
+/* (reference sources/gmlib3.c:2635-2663): first the link tables the kernel  */
+/* needs, each uplink followed by its degree table, then the user's          */
+/* datatypes in call order, each followed by its reference array when        */
+/* GmlRefFlag asks for it.  A kernel runs over entities of type `run`; a     */
+/* datatype of type `dst` is reached directly (same type), through a         */
+/* downlink (run has more dimensions, e.g. tet -> vertex: the element        */
+/* table), a same-dimension user link (e.g. neighbours), or an uplink (the   */
+/* ball of dst entities around each run entity).  The plan below is built    */
+/* from these rules; gml_codegen.c turns it into source.                     */
+/* ------------------------------------------------------------------------- */
+
+typedef struct
+{
+   int         dat, flags, link, count;   /* one user datatype of the kernel */
+}GmlUse;
+
+typedef struct
+{
+   GmlArgSct   arg[ GML_MAXARG ];
+   int         n;
+   int         up;                        /* index of the uplink argument, -1 if none */
+   int         high;                      /* its high-degree table, 0 if none */
+   int         width;                     /* that table's width */
+}GmlPlan;
+
+/* -1 downlink, 0 same dimension, +1 uplink */
+static int reach(int run, int dst)
+{
+   const int a = GmlMshTypDim[ run ], b = GmlMshTypDim[ dst ];
+   return a > b ? -1 : a < b ? 1 : 0;
+}
+
+static int plan_push(GmlPlan *p, GmlArgSct a)
+{
+   a.ArgIdx = p->n;
+   p->arg[ p->n ] = a;
+   return p->n++;
+}
+
+/* the latest argument bound to datatype `dat`, or -1 */
+static int plan_find(const GmlPlan *p, int dat)
+{
+   for(int j=p->n-1;j>=0;j--)
+      if(p->arg[j].DatIdx == dat)
+         return j;
+   return -1;
+}
+
+/* The default link of a run -> dst pair, built on first use under the
+   contract's names: <Run><Dst>Lnk/Deg for a downlink, <Run><Dst>Bal/Deg/Voy
+   for an uplink. */
+static int default_link(GmlSct *gml, int run, int dst, int dir)
+{
+   static const char *suffix[2][3] = { { "Lnk", "Deg", NULL }, { "Bal", "Deg", "Voy" } };
+   const char *nam[3] = { NULL, NULL, NULL };
+   char buf[ GmlMaxStrSiz ];
+
+   if(gml->LnkMat[ run ][ dst ])
+      return gml->LnkMat[ run ][ dst ];
+
+   for(int k=0;k<3;k++)
+      if(suffix[ dir > 0 ][k])
+      {
+         snprintf(buf, sizeof(buf), "%s%s%s", GmlBalTypStr[ run ], GmlBalTypStr[ dst ], suffix[ dir > 0 ][k]);
+         nam[k] = gmlx_intern(gml, buf);
+      }
+   if(!gml_new_ball_data(gml, run, dst, nam[0], nam[1], nam[2]))
+      return 0;
+   return gml->LnkMat[ run ][ dst ];
+}
+
+/* A link table as an argument: `width` entity indices per line, packed in
+   OpenCL int vectors. */
+static GmlArgSct link_arg(GmlSct *gml, int dat, int dst, int dir, int width)
+{
+   int cnt, len, typ;
+   gml_get_cnt_vec(width, &cnt, &len, &typ);
+   return (GmlArgSct){ .MshTyp = dst, .DatIdx = dat, .LnkTyp = -1, .LnkIdx = -1, .CntIdx = -1,
+                       .LnkDir = dir, .LnkDeg = dir > 0 ? -1 : width, .MaxDeg = width,
+                       .NmbItm = cnt, .ItmLen = len, .ItmTyp = typ, .FlgTab = GmlReadMode,
+                       .nam = gml->dat[ dat ].nam };
+}
+
+/* A user datatype (or its reference array) read through link argument `lk`
+   and count argument `ct` (either may be -1). */
+static GmlArgSct data_arg(const GmlPlan *p, const GmlDatSct *d, int dat, int lk, int ct, int flags)
+{
+   const GmlArgSct *l = lk >= 0 ? &p->arg[ lk ] : NULL;
+   return (GmlArgSct){ .MshTyp = d->MshTyp, .DatIdx = dat, .LnkDir = 0, .LnkTyp = d->MshTyp,
+                       .LnkIdx = lk, .CntIdx = ct,
+                       .LnkDeg = l && ct < 0 ? l->LnkDeg : -1, .MaxDeg = l ? l->MaxDeg : -1,
+                       .NmbItm = d->NmbItm, .ItmLen = d->ItmLen, .ItmTyp = d->ItmTyp,
+                       .FlgTab = flags, .nam = d->nam };
+}
+
+/* Link arguments, in the order of their first user.  Returns 0 when two
+   different uplinks would meet in one kernel (one high-degree twin only). */
+static int plan_links(GmlSct *gml, GmlPlan *p, int run, GmlUse *use, int nuse)
+{
+   for(int i=0;i<nuse;i++)
+   {
+      const int dst = gml->dat[ use[i].dat ].MshTyp;
+      const GmlDatSct *lnk;
+      int dir, width, at;
+
+      if(!use[i].link || plan_find(p, use[i].link) >= 0)
+         continue;
+
+      lnk   = &gml->dat[ use[i].link ];
+      dir   = reach(run, dst);
+      width = (lnk->AloTyp == GmlLnkDat && lnk->MshTyp == run && run == dst)
+            ? lnk->ItmLen : GmlLenMatBas[ run ][ dst ];
+      at    = plan_push(p, link_arg(gml, use[i].link, dst, dir, width));
+
+      if(dir <= 0)
+         continue;
+
+      /* an uplink: one kind per kernel, its voyeurs, then its degrees */
+      if(p->up >= 0 && p->high != gml->LnkHgh[ run ][ dst ])
+      {
+         puts("Current limitation prevents mixing two different kinds of uplink in the same kernel.");
+         return 0;
+      }
+      p->up    = at;
+      p->high  = gml->LnkHgh[ run ][ dst ];
+      p->width = gml->SizMatHgh[ run ][ dst ];
+      if(use[i].flags & GmlVoyeurs)
+      {
+         p->arg[ at ].VoyNam  = lnk->VoyNam;
+         p->arg[ at ].FlgTab |= GmlVoyeurs;
+         use[i].flags        &= ~GmlVoyeurs;
+      }
+      {
+         const int deg = gml->CntMat[ run ][ dst ];
+         plan_push(p, (GmlArgSct){ .MshTyp = dst, .DatIdx = deg, .LnkDir = 0, .LnkTyp = -1,
+                                   .LnkIdx = -1, .CntIdx = -1, .LnkDeg = 1, .MaxDeg = 1,
+                                   .NmbItm = 1, .ItmLen = 1, .ItmTyp = GmlInt,
+                                   .FlgTab = GmlReadMode, .nam = gml->dat[ deg ].nam });
+      }
+   }
+   return 1;
+}
+
+/* The user's datatypes, each with its reference array on request (not for
+   data read through a variable-degree uplink). */
+static void plan_data(GmlSct *gml, GmlPlan *p, const GmlUse *use, int nuse)
+{
+   for(int i=0;i<nuse;i++)
+   {
+      const GmlDatSct *d = &gml->dat[ use[i].dat ];
+      const int lk = use[i].link ? plan_find(p, use[i].link) : -1;
+      const int ct = use[i].count ? plan_find(p, use[i].count) : -1;
+      const int flags = use[i].flags & ~GmlRefFlag;
+      const int ref = gml->RefIdx[ d->MshTyp ];
+
+      plan_push(p, data_arg(p, d, use[i].dat, lk, ct, flags));
+      if((use[i].flags & GmlRefFlag) && ct < 0 && ref)
+         plan_push(p, data_arg(p, &gml->dat[ ref ], ref, lk, ct, flags));
+   }
+}
+
+/* bind a compiled kernel to the plan's datatypes and line range */
+static void bind_kernel(GmlKrnSct *krn, const GmlPlan *p, int lines, int first)
+{
+   krn->NmbDat    = p->n;
+   krn->NmbLin[0] = lines;
+   krn->NmbLin[1] = first;
+   for(int i=0;i<p->n;i++)
+      krn->DatTab[i] = p->arg[i].DatIdx;
+}
+
 int GmlCompileKernel(size_t GmlIdx, char *KrnSrc, char *PrcNam, int MshTyp, int NmbTyp, ...)
 {
    GETGMLPTR(gml, GmlIdx);
-   int i, j, flg, KrnIdx, KrnHghIdx, SrcTyp, DstTyp, NmbArg = 0, RefIdx;
-   int FlgTab[ GmlMaxDat ], IdxTab[ GmlMaxDat ], LnkTab[ GmlMaxDat ], CntTab[ GmlMaxDat ];
-   int LnkItm, NmbItm, ItmTyp, ItmLen, LnkPos, CptPos, RefFlg;
-   int NmbHgh = 0, HghVec, HghSiz, HghTyp, HghArg = -1, HghIdx = -1;
-   char BalNam[ GmlMaxStrSiz ], DegNam[ GmlMaxStrSiz ], VoyNam[ GmlMaxStrSiz ];
+   GmlUse use[ GmlMaxDat ];
+   GmlPlan plan;
    const char *ParSrc;
-   va_list VarArg;
-   GmlDatSct *dat, *RefDat;
-   GmlArgSct *arg, ArgTab[ GML_MAXARG ];
-   GmlKrnSct *krn;
+   int base, twin, lines, hlines;
+   va_list ap;
 
    if(MshTyp < 0 || MshTyp >= GmlMaxEleTyp || NmbTyp < 0 || NmbTyp > GmlMaxDat || !KrnSrc || !PrcNam)
       return 0;
 
-   ParSrc = gml->ParIdx ? gml->dat[ gml->ParIdx ].src : NULL;
-   memset(ArgTab, 0, sizeof(ArgTab));
-
-   va_start(VarArg, NmbTyp);
-   for(i=0;i<NmbTyp;i++)
+   /* (datatype, flags, link) triplets, as the reference's varargs */
+   va_start(ap, NmbTyp);
+   for(int i=0;i<NmbTyp;i++)
    {
-      IdxTab[i] = va_arg(VarArg, int);
-      FlgTab[i] = va_arg(VarArg, int);
-      LnkTab[i] = va_arg(VarArg, int);
-      CntTab[i] = 0;
+      use[i].dat   = va_arg(ap, int);
+      use[i].flags = va_arg(ap, int);
+      use[i].link  = va_arg(ap, int);
+      use[i].count = 0;
    }
-   va_end(VarArg);
+   va_end(ap);
 
-   for(i=0;i<NmbTyp;i++)
-      if(!chk_dat(gml, IdxTab[i]))
+   for(int i=0;i<NmbTyp;i++)
+   {
+      int dst, dir;
+
+      if(!chk_dat(gml, use[i].dat))
       {
-         printf("Invalid datatype index %d in kernel %s\n", IdxTab[i], PrcNam);
+         printf("Invalid datatype index %d in kernel %s\n", use[i].dat, PrcNam);
          return 0;
       }
-
-   /* check or build the default links (reference :2249-2289) */
-   for(i=0;i<NmbTyp;i++)
-   {
-      dat = &gml->dat[ IdxTab[i] ];
-
-      if(LnkTab[i] || dat->MshTyp == MshTyp)
+      dst = gml->dat[ use[i].dat ].MshTyp;
+      dir = reach(MshTyp, dst);
+      if(use[i].link || dst == MshTyp || !dir)
          continue;
-
-      SrcTyp = MshTyp;
-      DstTyp = dat->MshTyp;
-
-      if(GmlMshTypDim[ SrcTyp ] > GmlMshTypDim[ DstTyp ])
-      {
-         if(!gml->LnkMat[ MshTyp ][ DstTyp ])
-         {
-            snprintf(BalNam, sizeof(BalNam), "%s%sLnk", GmlBalTypStr[ MshTyp ], GmlBalTypStr[ DstTyp ]);
-            snprintf(DegNam, sizeof(DegNam), "%s%sDeg", GmlBalTypStr[ MshTyp ], GmlBalTypStr[ DstTyp ]);
-            if(!gml_new_ball_data(gml, MshTyp, DstTyp, gmlx_intern(gml, BalNam), gmlx_intern(gml, DegNam), NULL))
-               return 0;
-         }
-         LnkTab[i] = gml->LnkMat[ MshTyp ][ DstTyp ];
-         CntTab[i] = 0;
-      }
-      else if(GmlMshTypDim[ SrcTyp ] < GmlMshTypDim[ DstTyp ])
-      {
-         if(!gml->LnkMat[ MshTyp ][ DstTyp ])
-         {
-            snprintf(BalNam, sizeof(BalNam), "%s%sBal", GmlBalTypStr[ MshTyp ], GmlBalTypStr[ DstTyp ]);
-            snprintf(DegNam, sizeof(DegNam), "%s%sDeg", GmlBalTypStr[ MshTyp ], GmlBalTypStr[ DstTyp ]);
-            snprintf(VoyNam, sizeof(VoyNam), "%s%sVoy", GmlBalTypStr[ MshTyp ], GmlBalTypStr[ DstTyp ]);
-            if(!gml_new_ball_data(gml, MshTyp, DstTyp, gmlx_intern(gml, BalNam),
-                                  gmlx_intern(gml, DegNam), gmlx_intern(gml, VoyNam)))
-               return 0;
-         }
-         LnkTab[i] = gml->LnkMat[ MshTyp ][ DstTyp ];
-         CntTab[i] = gml->CntMat[ MshTyp ][ DstTyp ];
-      }
+      if(!(use[i].link = default_link(gml, MshTyp, dst, dir)))
+         return 0;
+      if(dir > 0)
+         use[i].count = gml->CntMat[ MshTyp ][ dst ];
    }
 
-   /* link arguments first (reference :2292-2398) */
-   for(i=0;i<NmbTyp;i++)
-   {
-      if(!LnkTab[i])
-         continue;
-
-      dat = &gml->dat[ IdxTab[i] ];
-      flg = 0;
-      for(j=0;j<NmbArg;j++)
-         if(ArgTab[j].DatIdx == LnkTab[i])
-            flg = 1;
-      if(flg)
-         continue;
-
-      SrcTyp = MshTyp;
-      DstTyp = dat->MshTyp;
-      LnkItm = GmlLenMatBas[ MshTyp ][ DstTyp ];
-
-      /* a user link gives its own width */
-      if(gml->dat[ LnkTab[i] ].AloTyp == GmlLnkDat && gml->dat[ LnkTab[i] ].MshTyp == MshTyp
-      && SrcTyp == DstTyp)
-         LnkItm = gml->dat[ LnkTab[i] ].ItmLen;
-
-      gml_get_cnt_vec(LnkItm, &NmbItm, &ItmLen, &ItmTyp);
-
-      arg = &ArgTab[ NmbArg ];
-      arg->ArgIdx = NmbArg++;
-      arg->MshTyp = DstTyp;
-      arg->DatIdx = LnkTab[i];
-      arg->LnkTyp = -1;
-      arg->LnkIdx = -1;
-      arg->CntIdx = -1;
-      arg->NmbItm = NmbItm;
-      arg->ItmLen = ItmLen;
-      arg->ItmTyp = ItmTyp;
-      arg->FlgTab = GmlReadMode;
-      arg->nam    = gml->dat[ arg->DatIdx ].nam;
-
-      if(GmlMshTypDim[ SrcTyp ] > GmlMshTypDim[ DstTyp ])
-      {
-         arg->LnkDir = -1;
-         arg->LnkDeg = LnkItm;
-         arg->MaxDeg = LnkItm;
-      }
-      else if(GmlMshTypDim[ SrcTyp ] == GmlMshTypDim[ DstTyp ])
-      {
-         arg->LnkDir = 0;
-         arg->LnkDeg = LnkItm;
-         arg->MaxDeg = LnkItm;
-      }
-      else
-      {
-         arg->LnkDir = 1;
-         arg->LnkDeg = -1;
-         arg->MaxDeg = LnkItm;
-
-         if(HghIdx != -1 && HghIdx != gml->LnkHgh[ MshTyp ][ DstTyp ])
-         {
-            puts("Current limitation prevents mixing two different kinds of uplink in the same kernel.");
-            return 0;
-         }
-
-         HghArg = arg->ArgIdx;
-         HghIdx = gml->LnkHgh[ MshTyp ][ DstTyp ];
-         NmbHgh = gml->SizMatHgh[ MshTyp ][ DstTyp ];
-
-         if(FlgTab[i] & GmlVoyeurs)
-         {
-            arg->VoyNam  = gml->dat[ arg->DatIdx ].VoyNam;
-            arg->FlgTab |= GmlVoyeurs;
-            FlgTab[i]   &= ~GmlVoyeurs;
-         }
-
-         /* degree (variable counter) argument */
-         arg = &ArgTab[ NmbArg ];
-         arg->ArgIdx = NmbArg++;
-         arg->MshTyp = DstTyp;
-         arg->DatIdx = gml->CntMat[ MshTyp ][ DstTyp ];
-         arg->LnkDir = 0;
-         arg->LnkTyp = -1;
-         arg->LnkIdx = -1;
-         arg->CntIdx = -1;
-         arg->LnkDeg = 1;
-         arg->MaxDeg = 1;
-         arg->NmbItm = 1;
-         arg->ItmLen = 1;
-         arg->ItmTyp = GmlInt;
-         arg->FlgTab = GmlReadMode;
-         arg->nam    = gml->dat[ arg->DatIdx ].nam;
-      }
-   }
-
-   /* data arguments (reference :2401-2499) */
-   for(i=0;i<NmbTyp;i++)
-   {
-      dat = &gml->dat[ IdxTab[i] ];
-      DstTyp = dat->MshTyp;
-      LnkPos = CptPos = -1;
-
-      if(LnkTab[i])
-         for(j=0;j<NmbArg;j++)
-            if(ArgTab[j].DatIdx == LnkTab[i])
-               LnkPos = j;
-
-      if(CntTab[i])
-         for(j=0;j<NmbArg;j++)
-            if(ArgTab[j].DatIdx == CntTab[i])
-               CptPos = j;
-
-      arg = &ArgTab[ NmbArg ];
-      arg->ArgIdx = NmbArg++;
-      arg->MshTyp = DstTyp;
-      arg->DatIdx = IdxTab[i];
-      arg->LnkDir = 0;
-      arg->LnkTyp = DstTyp;
-      arg->LnkIdx = LnkPos;
-      arg->CntIdx = CptPos;
-
-      if(LnkPos != -1 && CptPos != -1)
-      {
-         arg->LnkDeg = -1;
-         arg->MaxDeg = ArgTab[ LnkPos ].MaxDeg;
-      }
-      else if(LnkPos != -1)
-      {
-         arg->LnkDeg = ArgTab[ LnkPos ].LnkDeg;
-         arg->MaxDeg = ArgTab[ LnkPos ].MaxDeg;
-      }
-      else
-      {
-         arg->LnkDeg = -1;
-         arg->MaxDeg = -1;
-      }
-
-      RefFlg = (FlgTab[i] & GmlRefFlag) ? 1 : 0;
-      FlgTab[i] &= ~GmlRefFlag;
-
-      arg->NmbItm = dat->NmbItm;
-      arg->ItmLen = dat->ItmLen;
-      arg->ItmTyp = dat->ItmTyp;
-      arg->FlgTab = FlgTab[i];
-      arg->nam    = dat->nam;
-
-      if(!RefFlg || CptPos != -1 || !(RefIdx = gml->RefIdx[ DstTyp ]))
-         continue;
-
-      RefDat = &gml->dat[ RefIdx ];
-      arg = &ArgTab[ NmbArg ];
-      arg->ArgIdx = NmbArg++;
-      arg->MshTyp = DstTyp;
-      arg->DatIdx = RefIdx;
-      arg->LnkDir = 0;
-      arg->LnkTyp = DstTyp;
-      arg->LnkIdx = LnkPos;
-      arg->CntIdx = CptPos;
-      arg->LnkDeg = LnkPos != -1 ? ArgTab[ LnkPos ].LnkDeg : -1;
-      arg->MaxDeg = LnkPos != -1 ? ArgTab[ LnkPos ].MaxDeg : -1;
-      arg->NmbItm = RefDat->NmbItm;
-      arg->ItmLen = RefDat->ItmLen;
-      arg->ItmTyp = RefDat->ItmTyp;
-      arg->FlgTab = FlgTab[i];
-      arg->nam    = RefDat->nam;
-   }
-
-   KrnIdx = build_kernel(gml, KrnSrc, PrcNam, MshTyp, NmbArg, ArgTab, ParSrc);
-   if(!KrnIdx)
+   memset(&plan, 0, sizeof(plan));
+   plan.up = -1;
+   if(!plan_links(gml, &plan, MshTyp, use, NmbTyp))
       return 0;
+   plan_data(gml, &plan, use, NmbTyp);
 
-   krn = &gml->krn[ KrnIdx ];
-   krn->NmbDat    = NmbArg;
-   krn->NmbLin[1] = 0;
+   ParSrc = gml->ParIdx ? gml->dat[ gml->ParIdx ].src : NULL;
+   lines  = gml->dat[ gml->TypIdx[ MshTyp ] ].NmbLin;
+   hlines = plan.up >= 0 && plan.high > 0 ? gml->dat[ plan.high ].NmbLin : 0;
 
-   if(HghIdx <= 0)
-      krn->NmbLin[0] = gml->dat[ gml->TypIdx[ MshTyp ] ].NmbLin;
-   else
-      krn->NmbLin[0] = gml->dat[ gml->TypIdx[ MshTyp ] ].NmbLin - gml->dat[ HghIdx ].NmbLin;
-
-   for(i=0;i<NmbArg;i++)
-      krn->DatTab[i] = ArgTab[i].DatIdx;
-
-   if(HghArg == -1 || HghIdx <= 0)
-      return KrnIdx;
-
-   /* high-degree twin kernel (reference :2543-2589) */
-   gml_get_cnt_vec(NmbHgh, &HghVec, &HghSiz, &HghTyp);
-   ArgTab[ HghArg ].DatIdx = HghIdx;
-   ArgTab[ HghArg ].MaxDeg = NmbHgh;
-   ArgTab[ HghArg ].NmbItm = HghVec;
-   ArgTab[ HghArg ].ItmLen = HghSiz;
-   ArgTab[ HghArg ].ItmTyp = HghTyp;
-   for(i=0;i<NmbArg;i++)
-      if(ArgTab[i].LnkIdx == HghArg && ArgTab[i].CntIdx != -1)
-         ArgTab[i].MaxDeg = NmbHgh;
-
-   KrnHghIdx = build_kernel(gml, KrnSrc, PrcNam, MshTyp, NmbArg, ArgTab, ParSrc);
-   if(!KrnHghIdx)
+   if(!(base = build_kernel(gml, KrnSrc, PrcNam, MshTyp, plan.n, plan.arg, ParSrc)))
       return 0;
+   bind_kernel(&gml->krn[ base ], &plan, lines - hlines, 0);
+   if(!(plan.up >= 0 && plan.high > 0))
+      return base;
 
-   gml->krn[ KrnIdx ].HghIdx = KrnHghIdx;
-   krn = &gml->krn[ KrnHghIdx ];
-   krn->NmbDat    = NmbArg;
-   krn->NmbLin[0] = gml->dat[ HghIdx ].NmbLin;
-   krn->NmbLin[1] = gml->dat[ gml->TypIdx[ MshTyp ] ].NmbLin - gml->dat[ HghIdx ].NmbLin;
-
-   for(i=0;i<NmbArg;i++)
-      krn->DatTab[i] = ArgTab[i].DatIdx;
-
-   return KrnIdx;
+   /* The high-degree twin (reference :2543-2589): the same kernel over the
+      last hlines lines, reading the wide table; data gathered through it with
+      a variable degree get the wider bound. */
+   {
+      GmlArgSct *up = &plan.arg[ plan.up ];
+      int cnt, len, typ;
+      gml_get_cnt_vec(plan.width, &cnt, &len, &typ);
+      up->DatIdx = plan.high;
+      up->MaxDeg = plan.width;
+      up->NmbItm = cnt;
+      up->ItmLen = len;
+      up->ItmTyp = typ;
+      for(int i=0;i<plan.n;i++)
+         if(plan.arg[i].LnkIdx == plan.up && plan.arg[i].CntIdx != -1)
+            plan.arg[i].MaxDeg = plan.width;
+   }
+   if(!(twin = build_kernel(gml, KrnSrc, PrcNam, MshTyp, plan.n, plan.arg, ParSrc)))
+      return 0;
+   gml->krn[ base ].HghIdx = twin;
+   bind_kernel(&gml->krn[ twin ], &plan, hlines, lines - hlines);
+   return base;
 }
 
 /* ========================================================================= */
@@ -1596,34 +1503,31 @@ void   GmlDebugOff(size_t GmlIdx)          { GETGMLPTR(gml, GmlIdx); gml->DbgFlg
 /* Share of element-to-vertex accesses that hit a 16-entry direct-mapped
    cache of 1 KB lines (reference :4409-4442).  Like the reference, only the
    first node of each element line is looked at (it iterates j < NmbItm = 1). */
+/* How well the element -> vertex accesses of the mesh reuse a cache, in
+   percent of hits, by the reference's model (sources/gmlib3.c:4409-4442): a
+   direct-mapped cache of 16 sets; vertex v falls in set (v >> 4) mod 16 and is
+   tagged v >> 10 (bits 8-9 of v stay out of the tag); one lookup per item of
+   each element line, i.e. the line's first node, the mesh datatypes holding
+   one item per line; element types in increasing order from the edges. */
 float GmlEvaluateNumbering(size_t GmlIdx)
 {
    GETGMLPTR(gml, GmlIdx);
-   int typ, i, j, HshTab[64] = {0};
-   long long hit = 0, mis = 0;
+   int tag[16] = { 0 };
+   long long look = 0, hit = 0;
 
-   for(typ=GmlEdges; typ<GmlMaxEleTyp; typ++)
+   for(int typ=GmlEdges; typ<GmlMaxEleTyp; typ++)
    {
-      GmlDatSct *dat;
-      const int *EleTab;
-      if(!gml->TypIdx[ typ ])
-         continue;
-      dat = &gml->dat[ gml->TypIdx[ typ ] ];
-      EleTab = (const int *)dat->CpuMem;
-      for(i=0;i<dat->NmbLin;i++)
-         for(j=0;j<dat->NmbItm;j++)
+      const GmlDatSct *d = gml->TypIdx[ typ ] ? &gml->dat[ gml->TypIdx[ typ ] ] : NULL;
+      const int *node = d ? (const int *)d->CpuMem : NULL;
+
+      for(size_t e=0; node && e<(size_t)d->NmbLin; e++)
+         for(int k=0;k<d->NmbItm;k++, look++)
          {
-            int v = EleTab[ (size_t)i * dat->ItmLen + j ];
-            int pos = (v >> 4) & 0xf, adr = v >> 10;
-            if(HshTab[ pos ] == adr)
-               hit++;
-            else
-            {
-               mis++;
-               HshTab[ pos ] = adr;
-            }
+            const int v = node[ e * d->ItmLen + k ];
+            int *t = &tag[ (v >> 4) & 15 ];
+            hit += (*t == (v >> 10));
+            *t = v >> 10;
          }
    }
-
-   return (hit + mis) ? 100 * (float)hit / (float)(hit + mis) : 0.f;
+   return look ? 100 * (float)hit / (float)look : 0.f;
 }
