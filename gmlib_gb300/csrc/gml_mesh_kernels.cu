@@ -539,9 +539,11 @@ laplace_tma_kernel(int ntile, const unsigned *__restrict__ rowv, const long long
 /* mean-ratio quality, histogram, extrema, inverted flags                     */
 /* ========================================================================= */
 
+/* order-preserving key of a float, -0 folded onto +0 (ties between them go
+   to the smallest index) */
 __device__ __forceinline__ unsigned mk_fkey(float f)
 {
-   unsigned u = __float_as_uint(f);
+   unsigned u = __float_as_uint(f == 0.0f ? 0.0f : f);
    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 

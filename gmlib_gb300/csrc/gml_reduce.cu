@@ -21,8 +21,12 @@
  * non-zero values), L1 (sum of |x|), L2 (sum of x^2, no square root, as the
  * reference), Linf (max |x|).
  *
- * Scratch layout (device, bytes): [0,8) ticket counter, [8,16) result,
- * [16, 16 + 16*nblk) per-block partials (two doubles each).
+ * Scratch layout of gml_reduce_f32_kernel (device, bytes): [0,8) ticket
+ * counter, [8,16) result, [16, 16 + 8*nblk) per-block partials (one double
+ * each).  gml_minmax_arg_kernel has its own layout (see there).
+ *
+ * Line indices are 64-bit inside the kernels: with up to 2^31 - 1 lines, a
+ * grid-stride index can pass INT_MAX on its last step.
  */
 #include <cuda_runtime.h>
 #include <float.h>
@@ -83,18 +87,18 @@ gml_reduce_f32_kernel(const float *__restrict__ in, int n, unsigned long long *s
    __shared__ int last;
 
    float s = red_init<OP>(), c = 0.0f;
-   int tid = blockIdx.x * blockDim.x + threadIdx.x;
-   int nth = gridDim.x * blockDim.x;
-   int n4 = ((((uintptr_t)in) & 15) == 0) ? n >> 2 : 0;
+   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+   const long long nth = (long long)gridDim.x * blockDim.x;
+   const long long n4 = ((((uintptr_t)in) & 15) == 0) ? (long long)(n >> 2) : 0;
    const float4 *in4 = (const float4 *)in;
 
-   for(int i=tid;i<n4;i+=nth)
+   for(long long i=tid;i<n4;i+=nth)
    {
       float4 v = __ldg(&in4[i]);
       red_elem<OP>(v.x, s, c); red_elem<OP>(v.y, s, c);
       red_elem<OP>(v.z, s, c); red_elem<OP>(v.w, s, c);
    }
-   for(int i=4*n4+tid;i<n;i+=nth)
+   for(long long i=4*n4+tid;i<n;i+=nth)
       red_elem<OP>(__ldg(&in[i]), s, c);
 
    double d = (double)s + (double)c;
@@ -142,10 +146,13 @@ gml_reduce_f32_kernel(const float *__restrict__ in, int n, unsigned long long *s
 /* min / argmin / max / argmax with smallest-index ties                       */
 /* ------------------------------------------------------------------------- */
 
-/* order-preserving map of a float to an unsigned key */
+/* order-preserving map of a float to an unsigned key; -0 and +0 get the
+   same key, so that a tie between them goes to the smallest index.  A NaN
+   keeps its bit pattern's place: above +inf with the sign bit clear, below
+   -inf with it set. */
 __device__ __forceinline__ unsigned fkey(float f)
 {
-   unsigned u = __float_as_uint(f);
+   unsigned u = __float_as_uint(f == 0.0f ? 0.0f : f);
    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
@@ -163,10 +170,10 @@ gml_minmax_arg_kernel(const float *__restrict__ in, int n, unsigned long long *s
    __shared__ unsigned long long shmin[ RED_THREADS / 32 ], shmax[ RED_THREADS / 32 ];
    __shared__ int last;
    unsigned long long kmin = ~0ULL, kmax = ~0ULL;
-   int tid = blockIdx.x * blockDim.x + threadIdx.x;
-   int nth = gridDim.x * blockDim.x;
+   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+   const long long nth = (long long)gridDim.x * blockDim.x;
 
-   for(int i=tid;i<n;i+=nth)
+   for(long long i=tid;i<n;i+=nth)
    {
       unsigned k = fkey(__ldg(&in[i]));
       unsigned long long a = ((unsigned long long)k << 32) | (unsigned)i;

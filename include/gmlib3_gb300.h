@@ -136,9 +136,11 @@ int      GmlxReduceArg        (size_t, int DatIdx, float *MinVal, int *MinIdx,
  * device.  It is zero when the library's device code loads and every
  * completed call leaves it in that state; nothing needs clearing by the
  * caller.  Its address is looked up on the first call on each device, so
- * make that first call outside any stream capture.  Calls on one stream run
- * one after the other and are safe; calls that overlap on one device (two
- * streams, two host threads) share the scratch and race.
+ * make that first call outside any stream capture.  The looked-up address
+ * is kept for the life of the process: after cudaDeviceReset on a device
+ * the entry point must not be called on that device again.  Calls on one
+ * stream run one after the other and are safe; calls that overlap on one
+ * device (two streams, two host threads) share the scratch and race.
  * ------------------------------------------------------------------------- */
 #define GMLX_NOALLOC_MAX_LINES      2147483647      /* 32-bit line index */
 #define GMLX_NOALLOC_SCRATCH_BYTES  8208            /* (2 + 1024) x 8 bytes */

@@ -161,6 +161,25 @@ def test_reduction_ties_and_odd_sizes(G, O, gpu):
             G.lib.GmlStop(g)
 
 
+@pytest.mark.parametrize("first", [-0.0, 0.0])
+def test_argmin_signed_zero_ties(G, gpu, first):
+    """A minimum of zero held by -0.0 and +0.0 at several lines: the smallest
+    index wins whichever sign it carries (numpy's argmin agrees)."""
+    crd, tet, ref = G.cube_mesh(7, split=0, jitter=0.0, seed=1)
+    G.lib.GmlNewParameters(gpu, 8, PARAMS)
+    G.upload_mesh(gpu, crd, tet, ref)
+    q = G.lib.GmlNewSolutionData(gpu, G.GmlTetrahedra, 1, G.GmlFlt, b"qal")
+    x = np.ones(len(tet), np.float32)
+    x[1000], x[777], x[1500], x[2000] = -first, first, -0.0, 0.0
+    x[10], x[2040] = 5.0, 5.0                          # ties at the maximum too
+    G.set_data(gpu, q, x)
+    fmin, imin, fmax, imax = ctypes.c_float(), ctypes.c_int(), ctypes.c_float(), ctypes.c_int()
+    assert G.lib.GmlxReduceArg(gpu, q, ctypes.byref(fmin), ctypes.byref(imin),
+                               ctypes.byref(fmax), ctypes.byref(imax)) == 1
+    assert imin.value == 777 == int(np.argmin(x)) and fmin.value == 0.0
+    assert imax.value == 10 == int(np.argmax(x)) and fmax.value == 5.0
+
+
 def smoothing_step(G, g, v, nt, nv, lazy=1):
     G.lib.GmlxSetLazy(g, lazy)
     opt = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 4, G.GmlFlt4, b"OptCrd")

@@ -1,5 +1,7 @@
 """GmlxReduceNoAlloc (scratch in static device memory, nothing allocated)
-against GmlReduceVector on the same field, through the C ABI.
+against GmlReduceVector on the same field, and against numpy in FP64,
+through the C ABI; also on a field that starts 4 bytes past a 16-byte
+boundary (the kernel's scalar path).
 
 The file name sorts last so that the entry point also runs after every other
 test of the session; it passes alone in a fresh process as well."""
@@ -24,6 +26,14 @@ def _close(a, b, op):
     return abs(a - b) <= 1e-9 * max(1.0, abs(b))
 
 
+def _numpy(x, op):
+    """The same reductions in FP64 (sums of FP32 values are exact in FP64
+    up to rounding of the FP64 accumulation itself)."""
+    d = x.astype(np.float64)
+    return [d.min(), d.max(), d.sum(), float(np.count_nonzero(d)), np.abs(d).sum(),
+            (d * d).sum(), np.abs(d).max()][op]
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("n", [1, 1000, 3_000_001])
 def test_no_alloc_matches_reduce_vector(G, n):
@@ -41,11 +51,20 @@ def test_no_alloc_matches_reduce_vector(G, n):
         for op in OPS:
             want = ctypes.c_double()
             assert G.lib.GmlReduceVector(g, idx, op, ctypes.byref(want)) == 1
+            exact = _numpy(x, op)
+            assert _close(want.value, exact, op), (op, want.value, exact)
             for _ in range(2):                     # two calls in a row
                 got = ctypes.c_double(12345.0)
                 rc = G.lib.GmlxReduceNoAlloc(dev, n, op, ctypes.byref(got), stream)
                 assert rc == 1
                 assert _close(got.value, want.value, op), (op, got.value, want.value)
+                assert _close(got.value, exact, op), (op, got.value, exact)
+            if n > 1:
+                # lines 1..n-1: 4 bytes past the 16-byte boundary
+                got = ctypes.c_double()
+                assert G.lib.GmlxReduceNoAlloc(ctypes.c_void_p(dev + 4), n - 1, op,
+                                               ctypes.byref(got), stream) == 1
+                assert _close(got.value, _numpy(x[1:], op), op), (op, "unaligned")
     finally:
         G.lib.GmlStop(g)
 
