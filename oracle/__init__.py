@@ -189,6 +189,19 @@ def ref_p2_quality(crd, mid, tet, tedg):
     return out
 
 
+def ref_toolkit_table(pts):
+    """Every function of the reference's sources/toolkit.cl on point sets
+    pts (n, 8, 4) float32, through tests/kernels/toolkit_table.cl: (n, 64)
+    float32, or None where the reference tree is absent."""
+    r = refcl()
+    if r is None:
+        return None
+    pts = np.ascontiguousarray(pts, np.float32)
+    out = np.zeros((len(pts), 64), np.float32)
+    r.ref_toolkit_table(_ptr(pts), len(pts), _ptr(out))
+    return out
+
+
 def p2_quality(crd, mid, tet, tedg):
     """FP64 restatement of the P2 quality (orc_p2_quality)."""
     crd = np.ascontiguousarray(crd, np.float32)

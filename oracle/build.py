@@ -76,12 +76,13 @@ def build_refcl(force=False):
             os.path.join(REF_ROOT, "examples", "MeshQuality", "compute_quality.cl"),
             os.path.join(REF_ROOT, "examples", "NodeSmoothing", "scatter.cl"),
             os.path.join(REF_ROOT, "examples", "NodeSmoothing", "gather.cl"),
-            os.path.join(REF_ROOT, "examples", "P2Quality", "quality.cl")]
+            os.path.join(REF_ROOT, "examples", "P2Quality", "quality.cl"),
+            os.path.join(REPO, "tests", "kernels", "toolkit_table.cl")]
     if force or _stale(REF_LIB, deps):
         _run(["g++", "-O2", "-fPIC", "-shared", "-fopenmp", "-std=c++17",
               "-fsingle-precision-constant", "-ffp-contract=off",
               "-I" + os.path.join(HERE, "refcl"), "-I" + os.path.join(REF_ROOT, "sources"),
-              "-I" + os.path.join(REF_ROOT, "examples"),
+              "-I" + os.path.join(REF_ROOT, "examples"), "-I" + os.path.join(REPO, "tests", "kernels"),
               src, "-o", REF_LIB])
     return REF_LIB
 

@@ -6,7 +6,9 @@
  * (examples/MeshQuality/compute_quality.cl, examples/NodeSmoothing/scatter.cl
  * and gather.cl, examples/P2Quality/quality.cl), and wraps each body in the gather prologue and scatter
  * epilogue that the reference's generator writes around it
- * (sources/gmlib3.c:2739-2938), one loop iteration per work-item.  Built with
+ * (sources/gmlib3.c:2739-2938), one loop iteration per work-item; and a table
+ * of every toolkit function on given point sets (tests/kernels/toolkit_table.cl,
+ * this project's body, found through -I).  Built with
  * -fsingle-precision-constant like the reference's OpenCL build
  * (sources/gmlib3.c:2993).  Nothing from the reference is copied: the files
  * are compiled where they lie.
@@ -118,6 +120,26 @@ void ref_gather(float *crd, int nv, const int *deg, const int *ball, int width,
       for(int c=0;c<4;c++)
          crd[ 4 * (size_t)cnt + c ] = VerCrd.v[c];
 #undef OptCrdDegMax
+   }
+}
+
+/* every toolkit function on n point sets of 8 float4 (tests/kernels/
+   toolkit_table.cl), 64 results per set */
+void ref_toolkit_table(const float *pts, int n, float *res)
+{
+   #pragma omp parallel for schedule(static)
+   for(int cnt=0;cnt<n;cnt++)
+   {
+      float4 Pts[8];
+      float Res[64];
+      for(int k=0;k<8;k++)
+      {
+         const float *c = &pts[ 32 * (size_t)cnt + 4 * k ];
+         Pts[k] = float4(c[0], c[1], c[2], c[3]);
+      }
+#include "toolkit_table.cl"
+      for(int k=0;k<64;k++)
+         res[ 64 * (size_t)cnt + k ] = Res[k];
    }
 }
 

@@ -9,11 +9,16 @@ coordinates, residuals) plus the ball tables built by the reference's chained
 hash algorithm (oracle.c).  Tests then pin the oracle and the GPU path to
 these values on machines without the reference tree.
 
+toolkit.npz holds 512 jittered hexahedra (8 corners each, GMlib corner order)
+and the 64 results per hexahedron of tests/kernels/toolkit_table.cl, every
+function of the reference's sources/toolkit.cl, compiled from the reference
+tree and run on the CPU.
+
 p2_n5.npz holds a quadratic-tet mesh (gmlib_gb300.p2_mesh: vertices, unique
 edges with curved mid-edge nodes, the tet -> edge table) and the quality of
 the reference's examples/P2Quality/quality.cl body on it.
 
-Usage:  python tests/golden/make_golden.py [p2]     (p2: that fixture only)
+Usage:  python tests/golden/make_golden.py [p2|toolkit]   (one fixture only)
 """
 import os
 import sys
@@ -51,10 +56,32 @@ def make_p2(name, n, split, jitter, curve, seed):
     print(name, len(crd), len(tet), len(edges), "quality min %.6g mean %.6g" % (q.min(), q.mean()))
 
 
+def toolkit_points(n, seed):
+    """n unit hexahedra (corners 0-3 at z = 0 and 4-7 at z = 1, each face
+    counter-clockwise seen from outside the bottom) jittered by +-0.2."""
+    base = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
+                     [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], np.float64)
+    rng = np.random.default_rng(seed)
+    pts = np.zeros((n, 8, 4), np.float32)
+    pts[:, :, :3] = base[None] + rng.uniform(-0.2, 0.2, (n, 8, 3)) + rng.uniform(-5, 5, (n, 1, 3))
+    return pts
+
+
+def make_toolkit(name, n, seed):
+    pts = toolkit_points(n, seed)
+    res = O.ref_toolkit_table(pts)
+    np.savez_compressed(os.path.join(OUT, name), pts=pts, res=res)
+    print(name, pts.shape, res.shape)
+
+
 if __name__ == "__main__":
     if O.refcl() is None:
         sys.exit("the reference tree is needed to generate the golden fixtures")
-    if sys.argv[1:] != ["p2"]:
+    only = sys.argv[1] if len(sys.argv) > 1 else None
+    if only is None:
         make("kuhn_n5.npz", 5, 0, 0.25, 12345)
         make("reflected_n6.npz", 6, 1, 0.3, 777)
-    make_p2("p2_n5.npz", 5, 1, 0.15, 0.08, 4242)
+    if only in (None, "p2"):
+        make_p2("p2_n5.npz", 5, 1, 0.15, 0.08, 4242)
+    if only in (None, "toolkit"):
+        make_toolkit("toolkit.npz", 512, 31)
