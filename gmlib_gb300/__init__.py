@@ -168,6 +168,7 @@ SIGNATURES.update({
     "GmlxBatchFlags": (_i, [_s, _i, _p, _s]),
     "GmlxBatchTune": (_i, [_s, _i, _f]),
     "GmlxBatchSetTiles": (_i, [_s, _i, _i, _i, _i]),
+    "GmlxBatchSetWaitLimit": (_i, [_s, _i, _i]),
     "GmlxBatchInfo": (_i, [_s, _ip, _ip, _ip, _ip, _ip]),
     "GmlxServeNew": (_s, [_i, _d, _i]),
     "GmlxServeAddMesh": (_i, [_s, _i, _p, _p, _i, _p, _d]),

@@ -52,10 +52,15 @@ typedef struct
    void           *graph;
    int            gsweeps;
    float          gomega;
+   int            *hneed;                 /* host copy of need */
+   int            spin, hold;             /* wait limit; tiles held back (GmlxBatchSetWaitLimit) */
 }BatSct;
+
+#define BAT_SPIN (1 << 22)                 /* default wait limit: about 1 s */
 
 static void bat_free_tiles(GmlSct *gml, BatSct *b)
 {
+   free(b->hneed);              b->hneed = NULL;
    gmd_free(gml->dev, b->td);   b->td = NULL;
    gmd_free(gml->dev, b->need); b->need = NULL;
    gmd_free(gml->dev, b->done); b->done = NULL;
@@ -277,6 +282,15 @@ static int bat_tiles(GmlSct *gml, BatSct *b, int nsweeps)
       bat_free_tiles(gml, b);
       return 0;
    }
+   b->hneed = malloc((size_t)b->nmesh * nphase * sizeof(int));
+   if(!b->hneed)
+   {
+      free(t); free(need);
+      bat_free_tiles(gml, b);
+      return 0;
+   }
+   memcpy(b->hneed, need, (size_t)b->nmesh * nphase * sizeof(int));
+   need[0] += b->hold;
    gmd_h2d_async(gml->dev, b->td, t, (size_t)cnt * sizeof(GmdBatchTile));
    gmd_h2d_async(gml->dev, b->need, need, (size_t)b->nmesh * nphase * sizeof(int));
    gmd_sync(gml->dev);
@@ -365,6 +379,7 @@ static int bat_queue_work(GmlSct *gml, BatSct *b, NatSct *n, int nsweeps, float 
    a.flags = b->flags;
    a.stats = b->stats;
    a.omega = omega;
+   a.spin = b->spin > 0 ? b->spin : BAT_SPIN;
    return gmd_memset_async(gml->dev, b->ctl, 0, 2 * sizeof(int))
        && gmd_memset_async(gml->dev, b->done, 0, (size_t)b->nmesh * b->nphase * sizeof(int))
        && gmd_mesh_stats_init(gml->dev, b->stats, b->nmesh)
@@ -400,15 +415,20 @@ static int bat_loop_work(GmlSct *gml, BatSct *b, NatSct *n, int nsweeps, float o
    return !(nsweeps & 1) || gmd_d2d_async(gml->dev, vd->GpuMem, n->crd2, (size_t)b->nv * 16);
 }
 
+/* the device error bits of the last run, cleared once read so that the
+   instance runs on */
 static int bat_errors(GmlSct *gml, NatSct *n)
 {
    int err = 0;
    if(!gmd_d2h(gml->dev, &err, n->err, sizeof(int)))
       return -1;
+   if(err && !gmd_memset_async(gml->dev, n->err, 0, sizeof(int)))
+      return -1;
    if(err & 16)
       puts("GMlib: a batched tile waited too long for its dependencies; results are incomplete.");
    if(err & 4)
       puts("GMlib: a quality-kernel staging copy timed out; statistics are incomplete.");
+   fflush(stdout);
    return err & (16 | 4);
 }
 
@@ -462,6 +482,27 @@ int GmlxBatchRun(size_t GmlIdx, int nsweeps, float omega, int mode, GmlxQuality 
          return 0;
       for(int m=0;m<b->nmesh;m++)
          gmlx_decode_stats(&b->hstats[m], &res[m]);
+   }
+   return 1;
+}
+
+int GmlxBatchSetWaitLimit(size_t GmlIdx, int spin, int hold)
+{
+   GETGMLPTR(gml, GmlIdx);
+   BatSct *b = (BatSct *)gml->bat;
+
+   if(!b || spin < 0 || hold < 0)
+      return 0;
+   b->spin = spin;
+   b->hold = hold;
+   /* the queue launch is captured with its arguments: capture it again */
+   gmd_graph_free(b->graph);
+   b->graph = NULL;
+   if(b->td)
+   {
+      const int first = b->hneed[0] + hold;
+      if(!gmd_h2d_async(gml->dev, b->need, &first, sizeof(int)) || !gmd_sync(gml->dev))
+         return 0;
    }
    return 1;
 }

@@ -53,6 +53,7 @@ typedef struct
    unsigned             *flags;
    GmlxQualStats        *stats;
    float                omega;
+   int                  spin;        /* tries (about 256 ns each) before a waiting tile gives up */
 }GmdBatchArgs;
 
 int gmd_batch_queue(struct GmdCtx *ctx, const GmdBatchArgs *a, int grid);       /* block tiles */

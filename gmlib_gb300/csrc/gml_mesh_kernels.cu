@@ -278,44 +278,6 @@ __global__ void point_fill_kernel(int nrow, const int4 *__restrict__ tet, const 
 /* Laplacian sweep over the ball of points, one thread per SELL row           */
 /* ========================================================================= */
 
-__global__ void __launch_bounds__(MK_THREADS)
-laplace_sell_kernel(int nrow, const unsigned *__restrict__ rowv, const long long *__restrict__ soff,
-                    const int *__restrict__ col, const float4 *__restrict__ in,
-                    float4 *__restrict__ out, float omega)
-{
-   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-   if(r >= nrow) return;
-   const unsigned pk = __ldg(&rowv[r]);
-   if(pk == ROW_NONE) return;
-   const int v = (int)(pk & ROW_MASK), d = (int)(pk >> ROW_SHIFT);
-   const float4 p = __ldg(&in[v]);
-   if(d == 0)
-   {
-      out[v] = p;
-      return;
-   }
-   const int *cp = col + __ldg(&soff[r >> 5]) * 32 + (r & 31);
-   float sx = 0.f, sy = 0.f, sz = 0.f;
-   int k = 0;
-   for(;k+4<=d;k+=4)
-   {
-      const int c0 = __ldg(cp + (size_t)k * 32), c1 = __ldg(cp + (size_t)(k + 1) * 32);
-      const int c2 = __ldg(cp + (size_t)(k + 2) * 32), c3 = __ldg(cp + (size_t)(k + 3) * 32);
-      const float4 q0 = __ldg(&in[c0]), q1 = __ldg(&in[c1]), q2 = __ldg(&in[c2]), q3 = __ldg(&in[c3]);
-      sx += (q0.x + q1.x) + (q2.x + q3.x);
-      sy += (q0.y + q1.y) + (q2.y + q3.y);
-      sz += (q0.z + q1.z) + (q2.z + q3.z);
-   }
-   for(;k<d;k++)
-   {
-      const float4 q = __ldg(&in[ __ldg(cp + (size_t)k * 32) ]);
-      sx += q.x; sy += q.y; sz += q.z;
-   }
-   const float inv = 1.0f / (float)d;
-   out[v] = make_float4(p.x + omega * (sx * inv - p.x), p.y + omega * (sy * inv - p.y),
-                        p.z + omega * (sz * inv - p.z), 0.f);
-}
-
 /* The sweep as a persistent kernel: warp w handles slices w, w + W, ...
    and, before working on a slice, asks the TMA unit to prefetch the column
    block of its next slice into L2 (cp.async.bulk.prefetch.L2), so the
@@ -413,126 +375,6 @@ laplace_pf_kernel(int nslice, const unsigned *__restrict__ rowv, const long long
       out[v] = make_float4(p.x + omega * (sx * inv - p.x), p.y + omega * (sy * inv - p.y),
                            p.z + omega * (sz * inv - p.z), 0.f);
    }
-}
-
-/* The same sweep with the column block of each 256-row tile (8 slices,
-   contiguous in the SELL arrays) staged into shared memory by a TMA bulk
-   copy issued one tile ahead, so that the column stream never sits on the
-   gather chain: each thread reads its indices from shared memory and issues
-   its coordinate gathers back to back.  Tiles whose block exceeds the stage
-   capacity (balls wider than 32 on average in the tile) read their columns
-   from global memory instead. */
-#define LT_ROWS   SIGMA                       /* rows per tile */
-#define LT_CAP    (32 * 32 * (LT_ROWS / 32))  /* ints per stage: width <= 32 */
-#define LT_STAGES 2
-#define LT_SMEM   (LT_STAGES * LT_CAP * 4)
-
-__global__ void __launch_bounds__(LT_ROWS, 3)
-laplace_tma_kernel(int ntile, const unsigned *__restrict__ rowv, const long long *__restrict__ soff,
-                   const int *__restrict__ col, const float4 *__restrict__ in,
-                   float4 *__restrict__ out, float omega, int *err)
-{
-   extern __shared__ __align__(128) unsigned char lt_smem[];
-   __shared__ __align__(8) unsigned long long bar[LT_STAGES];
-   __shared__ long long toff[LT_STAGES][LT_ROWS / 32 + 1];
-   int *stage = (int *)lt_smem;
-   const int tid = threadIdx.x, lane = tid & 31, sl = tid >> 5;
-   const int mine = blockIdx.x < ntile ? (ntile - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-
-   /* thread 0 issues the copy of local tile i into stage i % LT_STAGES */
-   #define LT_ISSUE(i)                                                            \
-   {                                                                              \
-      const int tt = blockIdx.x + (i) * gridDim.x, ss = (i) % LT_STAGES;          \
-      const long long c0 = soff[ tt * (LT_ROWS / 32) ];                           \
-      const long long c1 = soff[ tt * (LT_ROWS / 32) + LT_ROWS / 32 ];            \
-      const unsigned bytes = (unsigned)((c1 - c0) * 128);                         \
-      if(bytes && bytes <= LT_CAP * 4)                                            \
-      {                                                                           \
-         mbar_expect_tx(&bar[ss], bytes);                                         \
-         tma_bulk_g2s(stage + ss * LT_CAP, col + c0 * 32, bytes, &bar[ss]);       \
-      }                                                                           \
-      else                                                                        \
-         mbar_expect_tx(&bar[ss], 0);                                             \
-   }
-
-   if(tid == 0)
-   {
-      for(int s=0;s<LT_STAGES;s++)
-         mbar_init(&bar[s], 1);
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-      for(int i=0;i<LT_STAGES && i<mine;i++)
-         LT_ISSUE(i);
-   }
-   __syncthreads();
-
-   for(int i=0;i<mine;i++)
-   {
-      const int t = blockIdx.x + i * gridDim.x, s = i % LT_STAGES;
-      const unsigned parity = (unsigned)((i / LT_STAGES) & 1);
-      if(tid <= LT_ROWS / 32)
-         toff[s][tid] = __ldg(&soff[ t * (LT_ROWS / 32) + tid ]);
-      const int r = t * LT_ROWS + tid;
-      const unsigned pk = __ldg(&rowv[r]);
-      const int ok = mbar_wait_bounded(&bar[s], parity);
-      if(__syncthreads_or(!ok))
-      {
-         if(tid == 0)
-         {
-            atomicOr(err, 8);
-            for(int j=i;j<mine && j<i+LT_STAGES;j++)
-               mbar_wait_bounded(&bar[j % LT_STAGES], (unsigned)((j / LT_STAGES) & 1));
-         }
-         __syncthreads();
-         return;
-      }
-
-      if(pk != ROW_NONE)
-      {
-         const int v = (int)(pk & ROW_MASK), d = (int)(pk >> ROW_SHIFT);
-         const float4 p = __ldg(&in[v]);
-         if(d == 0)
-            out[v] = p;
-         else
-         {
-            const long long base = toff[s][0];
-            const bool staged = (toff[s][LT_ROWS / 32] - base) * 32 <= LT_CAP;
-            const int *cp = staged ? stage + s * LT_CAP + (toff[s][sl] - base) * 32 + lane
-                                   : col + toff[s][sl] * 32 + lane;
-            float sx = 0.f, sy = 0.f, sz = 0.f;
-            int k = 0;
-            for(;k+8<=d;k+=8)
-            {
-               int c[8];
-               float4 q[8];
-#pragma unroll
-               for(int u=0;u<8;u++)
-                  c[u] = cp[(k + u) * 32];
-#pragma unroll
-               for(int u=0;u<8;u++)
-                  q[u] = __ldg(&in[ c[u] ]);
-#pragma unroll
-               for(int u=0;u<8;u++)
-               {
-                  sx += q[u].x; sy += q[u].y; sz += q[u].z;
-               }
-            }
-            for(;k<d;k++)
-            {
-               const float4 q = __ldg(&in[ cp[k * 32] ]);
-               sx += q.x; sy += q.y; sz += q.z;
-            }
-            const float inv = 1.0f / (float)d;
-            out[v] = make_float4(p.x + omega * (sx * inv - p.x), p.y + omega * (sy * inv - p.y),
-                                 p.z + omega * (sz * inv - p.z), 0.f);
-         }
-      }
-
-      /* all reads of stage s done: refill it with tile i + LT_STAGES */
-      __syncthreads();
-      if(tid == 0 && i + LT_STAGES < mine)
-         LT_ISSUE(i + LT_STAGES);
-   }
-   #undef LT_ISSUE
 }
 
 /* ========================================================================= */
@@ -973,51 +815,14 @@ extern "C" int gmd_mesh_laplace(GmdCtx *ctx, int nrow, const unsigned *rowv, con
                                 int bps)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
-   static int attr_set = 0, variant = -1;
-   const int ntile = nrow / LT_ROWS;
-   if(variant < 0)
-   {
-      /* GML_LAPLACE = sell, tma, pf or pf8 selects the sweep kernel (default pf8) */
-      const char *e = getenv("GML_LAPLACE");
-      variant = !e ? 3 : !strcmp(e, "sell") ? 1 : !strcmp(e, "tma") ? 0 : !strcmp(e, "pf") ? 2
-              : !strcmp(e, "pf16") ? 4 : 3;
-   }
-   if(variant >= 2)
-   {
-      const int nslice = nrow / 32;
-      long long need = nblk(nslice, MK_THREADS / 32);
-      long long cap2 = (long long)gmd_num_sms(ctx) * (bps > 0 && bps < LP_BLOCKS ? bps : LP_BLOCKS);
-      unsigned g2 = (unsigned)(need < cap2 ? need : cap2);
-      if(variant == 2)
-         laplace_pf_kernel<4><<<g2, MK_THREADS, 0, st>>>(nslice, rowv, soff, col, (const float4 *)in,
-                                                         (float4 *)out, omega);
-      else if(variant == 4)
-         laplace_pf_kernel<16><<<g2, MK_THREADS, 0, st>>>(nslice, rowv, soff, col, (const float4 *)in,
-                                                          (float4 *)out, omega);
-      else
-         laplace_pf_kernel<8><<<g2, MK_THREADS, 0, st>>>(nslice, rowv, soff, col, (const float4 *)in,
-                                                         (float4 *)out, omega);
-      return cudaGetLastError() == cudaSuccess;
-   }
-   if(variant == 1)
-   {
-      laplace_sell_kernel<<<nblk(nrow, MK_THREADS), MK_THREADS, 0, st>>>(nrow, rowv, soff, col,
-         (const float4 *)in, (float4 *)out, omega);
-      return cudaGetLastError() == cudaSuccess;
-   }
-   long long cap = (long long)gmd_num_sms(ctx) * 3;
-   unsigned g = (unsigned)(ntile < cap ? ntile : cap);
-   if(ntile <= 0)
+   const int nslice = nrow / 32;
+   const long long need = nblk(nslice, MK_THREADS / 32);
+   const long long cap = (long long)gmd_num_sms(ctx) * (bps > 0 && bps < LP_BLOCKS ? bps : LP_BLOCKS);
+   (void)err;
+   if(nslice <= 0)
       return 1;
-   if(!attr_set)
-   {
-      if(cudaFuncSetAttribute(laplace_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              LT_SMEM) != cudaSuccess)
-         return 0;
-      attr_set = 1;
-   }
-   laplace_tma_kernel<<<g, LT_ROWS, LT_SMEM, st>>>(ntile, rowv, soff, col, (const float4 *)in,
-                                                   (float4 *)out, omega, err);
+   laplace_pf_kernel<8><<<(unsigned)(need < cap ? need : cap), MK_THREADS, 0, st>>>(
+      nslice, rowv, soff, col, (const float4 *)in, (float4 *)out, omega);
    return cudaGetLastError() == cudaSuccess;
 }
 
@@ -1067,8 +872,9 @@ extern "C" int gmd_mesh_quality(GmdCtx *ctx, int nt, const void *tet, const void
    quality tiles), and a tile of phase p of mesh m starts only when all tiles
    of phase p - 1 of mesh m are done (per-(mesh, phase) counters).  A waiting
    tile only depends on tiles claimed before it, by blocks that are running,
-   so the queue always drains; the wait is nevertheless bounded and a
-   timeout aborts the launch with error bit 16.
+   so the queue always drains; the wait is nevertheless bounded (a.spin
+   tries of about 256 ns, 2^22 by default) and a timeout aborts the launch
+   with error bit 16.
 
    Coordinates written by other blocks of the same launch are read at L2
    (ld.global.cg), never through L1.  Sweep tiles are whole slices of the
@@ -1076,7 +882,6 @@ extern "C" int gmd_mesh_quality(GmdCtx *ctx, int nt, const void *tet, const void
    slices never mix meshes); quality tiles are tet ranges of one mesh starting
    at a multiple of 32, so each warp's ballot is one flag word of that mesh. */
 
-#define BQ_SPIN (1 << 22)
 
 __device__ __forceinline__ void batch_sweep_slices(int s0, int s1, const unsigned *__restrict__ rowv,
                                                    const long long *__restrict__ soff,
@@ -1203,7 +1008,7 @@ batch_queue_kernel(GmdBatchArgs a)
                int it = 0;
                while(*dp < need)
                {
-                  if(++it > BQ_SPIN || *(volatile int *)a.abort)
+                  if(++it > a.spin || *(volatile int *)a.abort)
                   {
                      atomicOr(a.err, 16);
                      *(volatile int *)a.abort = 1;
@@ -1419,7 +1224,7 @@ batch_warp_kernel(GmdBatchArgs a)
                int it = 0;
                while(*dp < need)
                {
-                  if(++it > BQ_SPIN || *(volatile int *)a.abort)
+                  if(++it > a.spin || *(volatile int *)a.abort)
                   {
                      atomicOr(a.err, 16);
                      *(volatile int *)a.abort = 1;

@@ -327,15 +327,11 @@ int GmlxInvertedFlags(size_t GmlIdx, unsigned *flags, size_t nwords)
 }
 
 /* resident blocks per SM of the quality pass and of the sweep when they run
-   side by side in the graph (0: each kernel's maximum; GML_SPLIT="q,l"
-   overrides, for tuning) */
+   side by side in the graph (0: each kernel's maximum) */
 static void graph_split(int *qb, int *lb)
 {
-   const char *e = getenv("GML_SPLIT");
    *qb = GML_SPLIT_Q;
    *lb = GML_SPLIT_L;
-   if(e && sscanf(e, "%d,%d", qb, lb) != 2)
-      *qb = *lb = 0;
 }
 
 int GmlxSmoothQualityLoop(size_t GmlIdx, int nsweeps, float omega, double h, GmlxQuality *res)

@@ -55,27 +55,24 @@ typedef struct
    double      *b64, *x64, *r64, *p64, *q64, *part, *spart;
    float       *d32, *r32, *p32[2], *q32;     /* p32[0], p32[1]: directions by parity */
    GmdSvScal   *sc, *hsc;        /* device scalars, pinned host copies (2 slots) */
-   void        *g64, *g32;       /* graphs of GML_CG_CHUNK iterations */
+   void        *g64, *g32;       /* graphs of `chunk` iterations */
    void        *ev[2], *t0, *t1;
    void        *tr[4];           /* phase and kernel timing of GML_CG_TRACE */
    int         chunk;            /* iterations per replay of g64 / g32 */
 }GmlSolver;
 
+/* the inner FP32 solve of the refinement loop stops when its residual has
+   fallen by this factor (10^-6 needed more iterations in total) */
 static double inner_factor(void)
 {
-   const char *e = getenv("GML_CG_INNER");
-   double f = e ? atof(e) : 0.;
-   return f > 0. && f < 1. ? f : 1e-5;
+   return 1e-5;
 }
 
-/* iterations per graph replay (GML_CG_CHUNK overrides, 2..64, rounded up
-   to even so that every replay starts on direction buffer 0) */
+/* iterations per graph replay, even so that every replay starts on
+   direction buffer 0 */
 static int cg_chunk(void)
 {
-   const char *e = getenv("GML_CG_CHUNK");
-   int c = e ? atoi(e) : 0;
-   c = c >= 1 && c <= 64 ? c : GML_CG_CHUNK;
-   return (c + 1) & ~1;
+   return (GML_CG_CHUNK + 1) & ~1;
 }
 
 static void solver_free(GmlSct *gml, GmlSolver *s)

@@ -7,6 +7,18 @@
  * the batched and served paths, and the controls of the launch machinery.
  * Each declaration names the reference function it extends, or says that it
  * has no counterpart in the reference.
+ *
+ * Environment variables read by the library (none changes a result):
+ *   GML_TUNE      at GmlInit: <= 0 turns block-size calibration off (block
+ *                 256), >= 32 fixes the block size; as GmlxSetTuning.
+ *   GML_LAZY      at GmlInit: 0 makes GmlCompileKernel always emit the
+ *                 reference's eager gather prologue; as GmlxSetLazy(0).
+ *   GML_DIRECT    at GmlInit: 0 keeps whole-datatype transfers on the staged
+ *                 path (host mirror, then DMA) instead of the one-kernel copy.
+ *   GML_CACHE_DIR a directory where compiled generated kernels are also kept
+ *                 on disk between processes (unset: in memory only).
+ *   GML_CG_TRACE  1 prints each GmlxSolveCG phase's wall and device time, 2
+ *                 each kernel's (timed one by one, without graphs).
  */
 #ifndef GMLIB3_GB300_H
 #define GMLIB3_GB300_H
@@ -241,6 +253,17 @@ int      GmlxBatchSetup       (size_t, int fix);
    launch loop.  res (may be NULL) receives NmbMsh results, tet indices local
    to each mesh.  The coordinates are updated in place. */
 int      GmlxBatchRun         (size_t, int nsweeps, float omega, int mode, GmlxQuality *res);
+
+/* The queue's dependency wait: a tile of sweep s + 1 waits on the device
+   until every sweep-s tile of its mesh is done, at most `spin` tries of
+   about 256 ns (0: the default 2^22, about 1 s); past that the launch stops,
+   GmlxBatchRun (given res) returns 0 and prints why, and the instance can
+   run again.  hold > 0 adds that many never-finished tiles to the first
+   sweep of mesh 0, so that its second-sweep tiles wait until the limit: a
+   host-side way to exercise the timeout (hold 0 restores the queue).  The
+   coordinates of a stopped run are incomplete.  No counterpart in the
+   reference. */
+int      GmlxBatchSetWaitLimit(size_t, int spin, int hold);
 
 /* Coordinates (4 floats per vertex) and inverted-element flags of a mesh. */
 int      GmlxBatchGetMesh     (size_t, int MshIdx, float *crd);

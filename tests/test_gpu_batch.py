@@ -163,3 +163,36 @@ def test_batch_rejects_bad_input():
         assert G.lib.GmlxBatchCreate(g, 1, G.as_ptr(nv), G.as_ptr(nt), G.as_ptr(h)) == 0
     finally:
         G.lib.GmlStop(g)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("warp", [0, 1])
+def test_batch_dependency_wait_times_out_and_recovers(capfd, warp):
+    """A queue whose first sweep of mesh 0 can never finish (one tile held
+    back on the host, GmlxBatchSetWaitLimit) with a wait limit of 4096 tries
+    (about 1 ms): the launch stops on its own with error bit 16,
+    GmlxBatchRun returns 0 and says why; with the limit and the queue
+    restored and the meshes set again, the same instance gives the results
+    of each mesh processed alone.  Nothing on the GPU faults or hangs: the
+    wait gives up and every block returns."""
+    ms = meshes()
+    g = make_batch(ms)
+    try:
+        if warp:
+            assert G.lib.GmlxBatchSetTiles(g, 1, 4, 1024, 0) == 1
+        res = (G.GmlxQuality * len(ms))()
+        assert G.lib.GmlxBatchSetWaitLimit(g, 4096, 1) == 1
+        assert G.lib.GmlxBatchRun(g, 2, OMEGA, G.GmlxBatchQueue, res) == 0
+        assert "waited too long" in capfd.readouterr().out
+        assert G.lib.GmlxBatchSetWaitLimit(g, 0, 0) == 1
+        for i, (n, crd, tet, ref) in enumerate(ms):
+            assert G.lib.GmlxBatchSetMesh(g, i, G.as_ptr(crd), G.as_ptr(ref), G.as_ptr(tet)) == 1
+        assert G.lib.GmlxBatchSetup(g, 1) == 1
+        assert G.lib.GmlxBatchRun(g, 2, OMEGA, G.GmlxBatchQueue, res) == 1
+        got = batch_results(g, ms)
+    finally:
+        G.lib.GmlStop(g)
+    for i, m in enumerate(ms):
+        c, q, fl = alone(*m, 2)
+        assert np.array_equal(got[i][0], c), i
+        same_quality(res[i], q)
