@@ -21,11 +21,11 @@
  * GmlImportMesh): Vertices 4, Edges 5, Triangles 6, Quadrilaterals 7,
  * Tetrahedra 8, Prisms 9, Hexahedra 10, Pyramids 49.
  *
- * GmlExportSolution writes the ASCII solution format (.sol): one
- * SolAtVertices / SolAtTetrahedra / ... keyword per mesh type, the field
- * count and a type code per field (1 scalar), one line per entity.  The
- * binary .solb encoding is not written (its solution keyword codes come
- * from libMeshb); asking for it fails with a message.
+ * GmlExportSolution writes the solution format, ASCII (.sol) or binary
+ * (.solb): one SolAtVertices / SolAtTetrahedra / ... keyword per mesh type,
+ * the field count and a type code per field (1 scalar), one line per entity.
+ * The keyword codes are libMeshb's (the library the reference links for its
+ * files, absent here; the Gamma Mesh Format as libMeshb 7 numbers it).
  */
 #include <ctype.h>
 #include <stdarg.h>
@@ -498,71 +498,140 @@ int GmlxExportMesh(size_t GmlIdx, const char *MshNam, int NmbTyp, const int *Typ
                                       : write_mesh_ascii(MshNam, gml, NmbTyp, TypTab);
 }
 
+/* libMeshb's solution keywords (SolAtVertices ... SolAtHexahedra), in the
+   enum element_type order, and its scalar field type code */
+static const int MioSolKwd[ GmlMaxEleTyp ] = { 62, 63, 64, 65, 66, 26, 67, 68 };
+#define MIO_SCA 1
+
+/* The float datatypes among DatTab that live on mesh type typ (at most 10,
+   all with the first one's line count): their indices in sel, the scalar
+   field count in *nfld, the line count returned (-1: none). */
+static int solution_fields(GmlSct *gml, int typ, int NmbDat, const int *DatTab, int *sel, int *ns,
+                           int *nfld)
+{
+   int nlin = -1;
+   *ns = *nfld = 0;
+   for(int k=0;k<NmbDat && *ns<10;k++)
+   {
+      const int di = DatTab[k];
+      const GmlDatSct *d;
+      if(di < 1 || di > GmlMaxDat || !gml->dat[di].use)
+         continue;
+      d = &gml->dat[di];
+      if(d->MshTyp != typ || (d->ItmTyp != GmlFlt && d->ItmTyp != GmlFlt2 && d->ItmTyp != GmlFlt4
+                              && d->ItmTyp != GmlFlt8 && d->ItmTyp != GmlFlt16))
+         continue;
+      if(nlin >= 0 && d->NmbLin != nlin)
+         continue;
+      nlin = d->NmbLin;
+      sel[ (*ns)++ ] = di;
+      *nfld += d->NmbItm * GmlTypVecSiz[ d->ItmTyp ];
+   }
+   for(int s=0;s<*ns;s++)
+      gml_download(gml, sel[s]);
+   return nlin;
+}
+
+/* the scalar fields of line i, in datatype then component order */
+static int line_values(GmlSct *gml, const int *sel, int ns, int i, double *out)
+{
+   int n = 0;
+   for(int s=0;s<ns;s++)
+   {
+      const GmlDatSct *d = &gml->dat[ sel[s] ];
+      const int nv = d->NmbItm * GmlTypVecSiz[ d->ItmTyp ];
+      const float *v = (const float *)((const char *)d->CpuMem + (size_t)i * d->LinSiz);
+      for(int c=0;c<nv;c++)
+         out[n++] = v[c];
+   }
+   return n;
+}
+
 /* Solution fields of the given datatypes, grouped by mesh type: each float
-   component of each datatype is one scalar field of its SolAt keyword. */
+   component of each datatype is one scalar field of its SolAt keyword.
+   Written in the ASCII encoding (.sol) or, for a .solb name, the binary one
+   of libMeshb's version 3 (int32 byte-order code 1 and version, then per
+   keyword: int32 code, int64 position of the next keyword, and for a SolAt
+   keyword the int32 line count, the int32 field count and one int32 type
+   code per field (1, scalar), then the lines as float64; Dimension 3 holds
+   int32 3; End (54) closes the file).  The reference writes through libMeshb
+   with the same keywords (sources/gmlib3.c:4591-4738); its ReferenceStrings
+   keyword, naming the fields, is not written here. */
 static int export_solution(size_t GmlIdx, const char *name, int NmbDat, const int *DatTab)
 {
    GETGMLPTR(gml, GmlIdx);
-   FILE *f;
-   int done = 0;
-   if(ends_with(name, ".solb"))
-   {
-      printf("GmlExportSolution: %s: only the ASCII .sol encoding is written\n", name);
-      fflush(stdout);
-      return 0;
-   }
-   if(!(f = fopen(name, "w")))
+   const int bin = ends_with(name, ".solb");
+   FILE *f = fopen(name, bin ? "wb" : "w");
+   int done = 0, ok = 1;
+   double *line = NULL;
+
+   if(!f)
    {
       printf("Could not create file %s\n", name);
       return 0;
    }
-   fprintf(f, "MeshVersionFormatted 2\n\nDimension 3\n");
-   for(int typ=0;typ<GmlMaxEleTyp;typ++)
+   if(bin)
    {
-      int sel[10], ns = 0, nfld = 0, nlin = -1;
-      for(int k=0;k<NmbDat;k++)
-      {
-         const int di = DatTab[k];
-         GmlDatSct *d;
-         if(di < 1 || di > GmlMaxDat || !gml->dat[di].use)
-            continue;
-         d = &gml->dat[di];
-         if(d->MshTyp != typ || (d->ItmTyp != GmlFlt && d->ItmTyp != GmlFlt2 && d->ItmTyp != GmlFlt4
-                                 && d->ItmTyp != GmlFlt8 && d->ItmTyp != GmlFlt16))
-            continue;
-         if(nlin >= 0 && d->NmbLin != nlin)
-            continue;
-         nlin = d->NmbLin;
-         sel[ns++] = di;
-         nfld += d->NmbItm * GmlTypVecSiz[ d->ItmTyp ];
-         if(ns == 10)
-            break;
-      }
-      if(!ns)
+      const int32_t hdr[2] = { 1, 3 }, dim[2] = { MIO_DIM, 0 };
+      const int64_t next = 8 + 4 + 8 + 4;
+      ok = fwrite(hdr, 4, 2, f) == 2 && fwrite(dim, 4, 1, f) == 1 && fwrite(&next, 8, 1, f) == 1
+        && fwrite(&(int32_t){ 3 }, 4, 1, f) == 1;
+   }
+   else
+      fprintf(f, "MeshVersionFormatted 2\n\nDimension 3\n");
+
+   for(int typ=0;typ<GmlMaxEleTyp && ok;typ++)
+   {
+      int sel[10], ns, nfld;
+      const int nlin = solution_fields(gml, typ, NmbDat, DatTab, sel, &ns, &nfld);
+      if(nlin < 0)
          continue;
-      fprintf(f, "\n%s\n%d\n%d", MioSolName[typ], nlin, nfld);
-      for(int i=0;i<nfld;i++)
-         fprintf(f, " 1");
-      fprintf(f, "\n");
-      for(int s=0;s<ns;s++)
-         gml_download(gml, sel[s]);
-      for(int i=0;i<nlin;i++)
+      free(line);
+      if(!(line = malloc((size_t)nfld * sizeof(double))))
       {
-         for(int s=0;s<ns;s++)
-         {
-            GmlDatSct *d = &gml->dat[ sel[s] ];
-            const int nv = d->NmbItm * GmlTypVecSiz[ d->ItmTyp ];
-            const float *v = (const float *)((const char *)d->CpuMem + (size_t)i * d->LinSiz);
-            for(int c=0;c<nv;c++)
-               fprintf(f, "%.9g ", v[c]);
-         }
+         ok = 0;
+         break;
+      }
+      if(bin)
+      {
+         const int64_t here = ftell(f);
+         const int64_t next = here + 4 + 8 + 4 + 4 + 4 * (int64_t)nfld + 8 * (int64_t)nfld * nlin;
+         const int32_t kwd = MioSolKwd[typ], nl = nlin, nf = nfld;
+         ok = fwrite(&kwd, 4, 1, f) == 1 && fwrite(&next, 8, 1, f) == 1 && fwrite(&nl, 4, 1, f) == 1
+           && fwrite(&nf, 4, 1, f) == 1;
+         for(int k=0;k<nfld && ok;k++)
+            ok = fwrite(&(int32_t){ MIO_SCA }, 4, 1, f) == 1;
+         for(int i=0;i<nlin && ok;i++)
+            ok = fwrite(line, 8, line_values(gml, sel, ns, i, line), f) == (size_t)nfld;
+         ok = ok && ftell(f) == next;
+      }
+      else
+      {
+         fprintf(f, "\n%s\n%d\n%d", MioSolName[typ], nlin, nfld);
+         for(int k=0;k<nfld;k++)
+            fprintf(f, " 1");
          fprintf(f, "\n");
+         for(int i=0;i<nlin;i++)
+         {
+            const int n = line_values(gml, sel, ns, i, line);
+            for(int c=0;c<n;c++)
+               fprintf(f, "%.9g ", line[c]);
+            fprintf(f, "\n");
+         }
       }
       done++;
    }
-   fprintf(f, "\nEnd\n");
-   fclose(f);
-   return done;
+   free(line);
+   if(bin)
+   {
+      const int32_t end = MIO_END;
+      const int64_t zero = 0;
+      ok = ok && fwrite(&end, 4, 1, f) == 1 && fwrite(&zero, 8, 1, f) == 1;
+   }
+   else
+      fprintf(f, "\nEnd\n");
+   ok = (fclose(f) == 0) && ok;
+   return ok ? done : 0;
 }
 
 int GmlxExportSolution(size_t GmlIdx, const char *SolNam, int NmbDat, const int *DatTab)

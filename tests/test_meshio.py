@@ -110,7 +110,55 @@ def test_solution_ascii(G, inst, tmp_path):
     assert words[k + 1:k + 4] == [str(len(tet)), "1", "1"]
     got = np.array([float(w) for w in words[k + 4:k + 4 + len(tet)]], np.float32)
     assert np.array_equal(got, vals)
-    assert G.lib.GmlxExportSolution(g, str(tmp_path / "q.solb").encode(), 1, d) == 0
+
+
+def read_solb(path):
+    """A version-3 binary solution file: {keyword: (lines, types, values)}."""
+    import struct
+    b = path.read_bytes()
+    code, ver = struct.unpack_from("<ii", b, 0)
+    assert code == 1 and ver == 3
+    pos, out = 8, {}
+    while True:
+        kwd, nxt = struct.unpack_from("<iq", b, pos)
+        if kwd == 54:
+            assert nxt == 0 and pos + 12 == len(b)
+            return out
+        if kwd == 3:
+            out[3] = struct.unpack_from("<i", b, pos + 12)[0]
+        else:
+            nl, nf = struct.unpack_from("<ii", b, pos + 12)
+            typ = np.frombuffer(b, np.int32, nf, pos + 20)
+            val = np.frombuffer(b, np.float64, nl * nf, pos + 20 + 4 * nf).reshape(nl, nf)
+            out[kwd] = (nl, typ, val)
+        pos = nxt
+
+
+def test_solution_binary(G, inst, tmp_path):
+    """The .solb encoding: Dimension 3, one SolAtTetrahedra (66) keyword with
+    one scalar field per float component (qal, then the 4 components of a
+    float4 field) and SolAtVertices (62) for a vertex field, float64 values
+    equal to the FP32 data."""
+    crd, tet, ref = G.cube_mesh(2, split=1, jitter=0.1, seed=2)
+    g = inst()
+    G.upload_mesh(g, crd, tet, ref)
+    q = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 1, G.GmlFlt, b"qal")
+    m = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 1, G.GmlFlt4, b"mid")
+    r = G.lib.GmlNewSolutionData(g, G.GmlVertices, 1, G.GmlFlt, b"res")
+    qv = np.arange(len(tet), dtype=np.float32) / 3
+    mv = np.random.default_rng(1).standard_normal((len(tet), 4)).astype(np.float32)
+    rv = np.linspace(-1, 1, len(crd)).astype(np.float32)
+    for idx, v in ((q, qv), (m, mv), (r, rv)):
+        assert G.set_data(g, idx, v) == 1
+    path = tmp_path / "s.solb"
+    assert G.lib.GmlxExportSolution(g, str(path).encode(), 3, (ctypes.c_int * 3)(q, m, r)) == 2
+    f = read_solb(path)
+    assert f[3] == 3
+    nl, typ, val = f[66]
+    assert nl == len(tet) and list(typ) == [1] * 5
+    assert np.array_equal(val, np.column_stack([qv, mv]).astype(np.float64))
+    nl, typ, val = f[62]
+    assert nl == len(crd) and list(typ) == [1] and np.array_equal(val[:, 0], rv.astype(np.float64))
 
 
 @pytest.mark.gpu
