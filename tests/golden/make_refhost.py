@@ -331,11 +331,128 @@ def make_linsolve():
     np.savez_compressed(os.path.join(OUT, "refhost_linsolve.npz"), **out)
 
 
+TET_FACES = ((1, 2, 3), (2, 0, 3), (3, 0, 1), (0, 2, 1))
+
+
+def boundary_triangles(crd, tet):
+    """The boundary faces of a cube mesh as triangles, each referenced by its
+    cube side: 1/2 for x = 0/1, 3/4 for y, 5/6 for z, in tet then face order."""
+    seen = {}
+    for i, t in enumerate(tet):
+        for j, f in enumerate(TET_FACES):
+            key = tuple(sorted(t[list(f)]))
+            seen[key] = None if key in seen else (i, j)
+    tri, ref = [], []
+    for key, v in seen.items():
+        if v is None:
+            continue
+        i, j = v
+        nodes = tet[i][list(TET_FACES[j])]
+        c = crd[nodes, :3]
+        for axis in range(3):
+            for side in (0, 1):
+                if np.all(np.abs(c[:, axis] - side) < 1e-6):
+                    ref.append(1 + 2 * axis + side)
+        tri.append(nodes)
+    return np.array(tri, np.int32), np.array(ref, np.int32)
+
+
+HEAT_ITERS = 30
+
+
+def heat_mesh():
+    import gmlib_gb300 as G
+    crd, tet, ref = G.cube_mesh(4, split=0, jitter=0.2, seed=77)
+    tri, tref = boundary_triangles(crd, tet)
+    return crd, tet, ref, tri, tref
+
+
+def heat_parameters():
+    """The example's parameter block (HeatCellCentered.c:80): boundary types
+    (DIRICHLET 0, NEUMANN 1) of sides 1..6, their references, their values."""
+    import struct
+    return struct.pack("6i6i6ff", 1, 1, 1, 0, 0, 1, 1, 2, 3, 4, 5, 6,
+                       0., 0., 0., 300., 250., 0., 0.)
+
+
+def make_heat():
+    """The HeatCellCentered flow (HeatCellCentered.c:90-180) with the
+    example's own kernel bodies: faces, the triangle -> tet shells and tet ->
+    triangle links those kernels build, the time step and HEAT_ITERS
+    iterations, with the cell values, face values and residual norms."""
+    crd, tet, ref, tri, tref = heat_mesh()
+    I = R.Instance()
+    par = heat_parameters()
+    p = I.parameters(len(par), body("HeatCellCentered/param.cl"))
+    ctypes.memmove(p, par, len(par))
+    v = I.mesh(R.GmlVertices, crd, ref)
+    I.mesh(R.GmlTetrahedra, tet)
+    I.mesh(R.GmlTriangles, tri, tref)
+    nf = I.L.GmlExtractFaces(I.g)
+    ntri, t = I.mesh_info(R.GmlTriangles)
+    assert nf == ntri
+    faces = I.get_lines(t, ntri, "iii").astype(np.int32)
+    nt = len(tet)
+    sol = I.solution(R.GmlTetrahedra, 1, R.GmlFlt, b"SolTet")
+    grd = I.solution(R.GmlTetrahedra, 1, R.GmlFlt4, b"GrdTet")
+    sext = I.solution(R.GmlTriangles, 1, R.GmlFlt, b"SolExt")
+    gext = I.solution(R.GmlTriangles, 1, R.GmlFlt4, b"GrdExt")
+    rhs = I.solution(R.GmlTetrahedra, 1, R.GmlFlt, b"Rhs")
+    dt = I.solution(R.GmlTetrahedra, 1, R.GmlFlt, b"dt")
+    first = R.lib().refhost_nkernels()
+    K = {}
+    K["sol_ext"] = I.compile(body("HeatCellCentered/sol_ext.cl"), b"sol_ext", R.GmlTriangles,
+                             [(t, R.GmlReadMode | R.GmlRefFlag), (sol, R.GmlReadMode),
+                              (sext, R.GmlWriteMode)])
+    K["grd_tet"] = I.compile(body("HeatCellCentered/grd_tet.cl"), b"grd_tet", R.GmlTetrahedra,
+                             [(v, R.GmlReadMode), (sext, R.GmlReadMode), (grd, R.GmlWriteMode)])
+    K["grd_ext"] = I.compile(body("HeatCellCentered/grd_ext.cl"), b"grd_ext", R.GmlTriangles,
+                             [(t, R.GmlReadMode | R.GmlRefFlag), (grd, R.GmlReadMode),
+                              (gext, R.GmlWriteMode)])
+    K["flx_bal"] = I.compile(body("HeatCellCentered/flx_bal.cl"), b"flx_bal", R.GmlTetrahedra,
+                             [(v, R.GmlReadMode), (gext, R.GmlReadMode), (rhs, R.GmlWriteMode)])
+    K["tim_int"] = I.compile(body("HeatCellCentered/tim_int.cl"), b"tim_int", R.GmlTetrahedra,
+                             [(rhs, R.GmlReadMode), (sol, R.GmlReadMode | R.GmlWriteMode)])
+    K["dt"] = I.compile(body("HeatCellCentered/dt.cl"), b"dt", R.GmlTetrahedra,
+                        [(v, R.GmlReadMode), (dt, R.GmlWriteMode)])
+    obj = {n: [k for k in R.kernel_objects(n) if k >= first][0] for n in K}
+    I.launch(K["dt"])
+    dtmin = I.reduce(dt, R.GmlMin)
+    # GmlPar->dt, then GmlUploadParameters (HeatCellCentered.c:166-169)
+    ctypes.memmove(p + 72, np.float32(dtmin).tobytes(), 4)
+    assert I.L.GmlUploadParameters(I.g) == 1
+    res = []
+    for _ in range(HEAT_ITERS):
+        for n in ("sol_ext", "grd_tet", "grd_ext", "flx_bal", "tim_int"):
+            I.launch(K[n])
+        res.append(I.reduce(rhs, R.GmlL2))
+    sb = R.kernel_buffers(obj["sol_ext"])
+    gb = R.kernel_buffers(obj["grd_tet"])
+    out = dict(crd=crd, tet=tet, ref=ref, tri=tri, tref=tref, faces=faces,
+               dt=np.float32(dtmin), res=np.array(res),
+               sol=f32(R.kernel_buffers(obj["tim_int"])["SolTetTab"], (nt,)),
+               sext=f32(sb["SolExtTab"], (ntri,)),
+               grd=f32(gb["GrdTetTab"], (nt, 4)))
+    # the link tables the kernels read: triangle -> tet shells (entries
+    # (tet << 4) | local face, degree per triangle) and tet -> triangle faces
+    names = R.kernel_signature(obj["sol_ext"])
+    shl = [n for n in names if n.endswith("BalTab")][0]
+    deg = [n for n in names if n.endswith("DegTab")][0]
+    out["shell"] = np.frombuffer(sb[shl], np.int32)[:2 * ntri].reshape(ntri, 2).copy()
+    out["shell_deg"] = np.frombuffer(sb[deg], np.int32)[:ntri].copy()
+    lnk = [n for n in R.kernel_signature(obj["grd_tet"]) if n.endswith("LnkTab")][0]
+    out["tet_faces"] = np.frombuffer(gb[lnk], np.int32)[:4 * nt].reshape(nt, 4).copy()
+    np.savez_compressed(os.path.join(OUT, "refhost_heat.npz"), **out)
+    print("refhost_heat.npz", ntri, "faces", shl, deg, lnk, "dt", dtmin, "res", res[0], res[-1])
+    I.stop()
+
+
 CASES = {
     "kuhn_n5": lambda: make_case("refhost_kuhn_n5.npz", "kuhn_n5.npz"),
     "reflected_n6": lambda: make_case("refhost_reflected_n6.npz", "reflected_n6.npz"),
     "linsolve": make_linsolve,
     "c1": make_c1,
+    "heat": make_heat,
 }
 
 if __name__ == "__main__":
