@@ -224,23 +224,31 @@ def workload_config(n, nv, nt, wset_mb, degrees=None):
 # ---------------------------------------------------------------- CPU port
 
 def cpu_port(crd, tet, ref, nsweeps, reps):
-    """Time the oracle's OpenMP port: nsweeps sweep+quality passes, reps
-    times; returns (seconds per pass list, threads)."""
+    """Time the oracle's OpenMP port: reps steps of nsweeps sweep+quality
+    passes, each from the mesh's initial coordinates; returns (seconds per
+    step list, threads, ball entries, the first step's result: coordinates,
+    last-sweep histogram, minimum, argmin, inverted count)."""
     import oracle as O
     lib = O.lib()
     fixed = (ref != 0).astype(np.int32)
     ptr, col = O.point_ball(len(crd), tet, fixed)
-    c = np.array(crd, np.float32, copy=True)
-    tmp = np.zeros_like(c)
+    tmp = np.zeros((len(crd), 4), np.float32)
     hist = np.zeros(64 * nsweeps, np.uint32)
-    ts = []
-    for _ in range(reps):
+    qmin = np.zeros(nsweeps, np.float32)
+    imin = np.zeros(nsweeps, np.int32)
+    ninv = np.zeros(nsweeps, np.uint32)
+    ts, first = [], None
+    for r in range(reps):
+        c = np.array(crd, np.float32, copy=True)
         t0 = time.perf_counter()
         lib.orc_bench_step(len(c), len(tet), O._ptr(c), O._ptr(tmp), O._ptr(tet), O._ptr(ptr),
-                           O._ptr(col), ctypes.c_float(OMEGA), nsweeps, O._ptr(hist), None,
-                           None, None)
-        ts.append((time.perf_counter() - t0) / nsweeps)
-    return ts, lib.orc_threads(), len(col)
+                           O._ptr(col), ctypes.c_float(OMEGA), nsweeps, O._ptr(hist),
+                           O._ptr(qmin), O._ptr(imin), O._ptr(ninv))
+        ts.append(time.perf_counter() - t0)
+        if r == 0:
+            first = {"crd": c, "hist": hist[-64:].copy(), "min": float(qmin[-1]),
+                     "argmin": int(imin[-1]), "inverted": int(ninv[-1])}
+    return ts, lib.orc_threads(), len(col), first
 
 
 def step_bytes_host(nv, nt, used):
@@ -252,26 +260,28 @@ def step_bytes_host(nv, nt, used):
 # ------------------------------------------------------------- reference arm
 
 def run_reference(args, dist):
+    """The reference arm: the same step as the GPU arm (SWEEPS Jacobi sweeps,
+    each followed by the quality pass with histogram, minimum and inverted
+    count) on the same mesh, by the oracle's OpenMP port on every host core,
+    --warmup untimed and --steps timed whole steps."""
     if dist.rank != 0:
         return
     n = args.n
     crd, tet, ref = mesh(n)
-    steps = min(args.steps, 20)
-    warm = min(args.warmup, 3)
-    ts, threads, used = cpu_port(crd, tet, ref, 1, warm + steps)
-    ts = ts[warm:]
+    ts, threads, used, _ = cpu_port(crd, tet, ref, SWEEPS, args.warmup + args.steps)
+    ts = ts[args.warmup:]
     sweep, qual = step_bytes_host(len(crd), len(tet), used)
     per = statistics.median(ts)
-    value = (sweep + qual) / per / 1e9
-    wset = (16.0 * len(tet) + 32.0 * len(crd) + 4.0 * used) / 1e6
-    sample = ("one sweep + one quality pass (1/%d of a step) on the full mesh per timed "
-              "step, %d timed steps" % (SWEEPS, steps))
+    value = SWEEPS * (sweep + qual) / per / 1e9
+    sample = "the whole step (%d sweeps + %d quality passes) on the full mesh, median of %d " \
+             "timed steps" % (SWEEPS, SWEEPS, args.steps)
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s",
-            "n_gpus": args.gpus, "steps": steps, "warmup": warm,
-            "ms_per_step": round(per * SWEEPS * 1e3, 3), "higher_is_better": True,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(per * 1e3, 3), "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(n, len(crd), len(tet), wset, degree_summary([tet])),
+            "config": workload_config(n, len(crd), len(tet), working_set(len(crd), len(tet), used),
+                                      degree_summary([tet])),
             "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads,
                              "kind": "port", "sample": sample},
             "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
@@ -280,6 +290,12 @@ def run_reference(args, dist):
                     "runtime exists on this box, so its CPU path is the oracle's "
                     "OpenMP port of the same workload"}
     print(json.dumps(line), flush=True)
+
+
+def working_set(nv, nt, used):
+    """MB read per step-pass of the workload, the same for both arms: tets,
+    coordinates read and written, ball entries."""
+    return (16.0 * nt + 32.0 * nv + 4.0 * used) / 1e6
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -305,7 +321,7 @@ def run_gpu(args, dist):
     step_bytes = SWEEPS * (sweep_b.value + qual_b.value)
     stored, used, mx = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
     G.lib.GmlxMeshBallInfo(g, ctypes.byref(stored), ctypes.byref(used), ctypes.byref(mx))
-    wset = (16.0 * nt + 32.0 * nv + 4.0 * stored.value) / 1e6
+    wset = working_set(nv, nt, used.value)
     res = (G.GmlxQuality * SWEEPS)()
     om = ctypes.c_float(OMEGA)
 
@@ -379,14 +395,34 @@ def run_gpu(args, dist):
            "d2h_bytes_per_step": out_crd.nbytes + SWEEPS * ctypes.sizeof(G.GmlxQuality),
            "ms_per_step": round(e2e_s * 1e3, 3)}
 
-    cpu = None
+    # one step from the initial coordinates, kept for the check below
+    G.lib.GmlxSetData(g, vidx, G.as_ptr(host_crd), host_crd.nbytes)
+    G.lib.GmlxSmoothQualityLoop(g, SWEEPS, om, h, res)
+    first_crd = np.empty_like(host_crd)
+    G.lib.GmlxGetData(g, vidx, G.as_ptr(first_crd), first_crd.nbytes)
+    first = res[SWEEPS - 1]
+
+    cpu, check = None, None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        ts, threads, cused = cpu_port(crd, tet, ref, 1, 3)
+        # the CPU baseline: whole steps of the port; its first step, from the
+        # same initial coordinates, is also the checker of the GPU's first step
+        ts, threads, cused, port = cpu_port(crd, tet, ref, SWEEPS, 3)
         sw, qu = step_bytes_host(nv, nt, cused)
-        cpu = {"value": round((sw + qu) / statistics.median(ts) / 1e9, 3), "unit": "GB/s",
+        cpu = {"value": round(SWEEPS * (sw + qu) / statistics.median(ts) / 1e9, 3), "unit": "GB/s",
                "cores": threads, "kind": "port",
-               "sample": "one sweep + one quality pass (1/%d of a step) on the full mesh, "
-                         "median of 3" % SWEEPS}
+               "sample": "the whole step (%d sweeps + %d quality passes) on the full mesh, "
+                         "median of 3" % (SWEEPS, SWEEPS)}
+        dx = float(np.max(np.abs(first_crd[:, :3] - port["crd"][:, :3])))
+        hd = int(np.abs(np.array(first.Hist[:], np.int64) - port["hist"].astype(np.int64)).sum())
+        check = {"against": "the CPU port's step from the same coordinates (FP32)",
+                 "max_coordinate_diff": dx, "histogram_abs_diff": hd,
+                 "min": [first.MinQal, port["min"]], "argmin": [first.MinIdx, port["argmin"]],
+                 "inverted": [first.NmbInv, port["inverted"]],
+                 "pass": bool(dx <= 2e-6 and hd <= 8 and first.MinIdx == port["argmin"]
+                              and abs(first.MinQal - port["min"]) <= 2e-5
+                              and first.NmbInv == port["inverted"])}
+
+    others = other_configs(G, dev) if dist.world == 1 else None
 
     G.lib.GmlStop(g)
 
@@ -403,8 +439,74 @@ def run_gpu(args, dist):
                                  "inverted": last.NmbInv, "fp64_determinants": last.NmbF64,
                                  "ball_entries_used": used.value,
                                  "ball_entries_stored": stored.value,
-                                 "max_ball_of_points": mx.value}}
+                                 "max_ball_of_points": mx.value,
+                                 "first_step_check": check},
+                "other_configs": others}
         print(json.dumps(line), flush=True)
+
+
+def other_configs(G, dev):
+    """Compact results of the plain-quality configuration (32^3-hex Kuhn
+    cube, 196,608 tets: one quality pass with statistics, L2 flushed before
+    each of 20 launches) and of the solver configuration (96^3-hex SPD
+    block system: FP64 CG and FP32 CG inside FP64 refinement to 1e-10,
+    median of 3 solves after one), for the default run."""
+    out = {}
+    n = Q_N
+    crd, tet, ref = G.cube_mesh(n, split=0, jitter=Q_JITTER, seed=Q_SEED)
+    g = G.lib.GmlInit(dev)
+    if not g:
+        raise SystemExit("GmlInit failed")
+    G.lib.GmlxSetTiming(g, 0)
+    G.upload_mesh(g, crd, tet, ref)
+    if G.lib.GmlxMeshSetup(g, 1) != 1:
+        raise SystemExit("GmlxMeshSetup failed")
+    flush = G.lib.GmlNewVector(g, 16 << 20, 4, None, G.GmlFlt)
+    one = ctypes.c_double(1.0)
+    e0, e1 = G.lib.GmlxEventCreate(), G.lib.GmlxEventCreate()
+    res = G.GmlxQuality()
+    for _ in range(3):
+        G.lib.GmlxQualityStats(g, 1.0 / n, 0, None)
+    tot = 0.0
+    for _ in range(20):
+        G.lib.GmlScaleVec(g, flush, ctypes.byref(one))
+        G.lib.GmlxEventRecord(g, e0)
+        G.lib.GmlxQualityStats(g, 1.0 / n, 0, None)
+        G.lib.GmlxEventRecord(g, e1)
+        tot += G.lib.GmlxEventElapsed(e0, e1)
+    G.lib.GmlxQualityStats(g, 1.0 / n, 0, ctypes.byref(res))
+    G.lib.GmlStop(g)
+    out["quality_32cube"] = {"metric": "tet qualities per second", "unit": "M tets/s",
+                             "value": round(len(tet) / (tot / 20) / 1e6, 2),
+                             "mean_launch_us": round(tot / 20 * 1e6, 2),
+                             "min": res.MinQal, "argmin": res.MinIdx, "inverted": res.NmbInv}
+    lin, col, val, rhs = G.cube_spd(SOLVE_N, 0, seed=SEED)
+    nrow, nnzb = len(lin) - 1, len(col)
+    g = G.lib.GmlInit(dev)
+    G.lib.GmlxSetTiming(g, 0)
+    IP = ctypes.POINTER(ctypes.c_int)
+    v64 = np.ascontiguousarray(val)
+    m64 = G.lib.GmlNewMatrix(g, nrow, nnzb, 3, G.as_ptr(v64), col.ctypes.data_as(IP),
+                             lin.ctypes.data_as(IP), G.GmlDbl)
+    vb = G.lib.GmlNewVector(g, nrow, 3, G.as_ptr(rhs), G.GmlDbl)
+    vx = G.lib.GmlNewVector(g, nrow, 3, None, G.GmlDbl)
+    solves = {}
+    for mode, name in ((G.GmlxCgFp64, "cg_fp64"), (G.GmlxCgMixed, "cg_fp32_in_fp64_ir")):
+        info = G.GmlxSolveInfo()
+        times = []
+        for i in range(4):
+            if G.lib.GmlxSolveCG(g, m64, vb, vx, mode, SOLVE_TOL, 20000, ctypes.byref(info)) != 1:
+                raise SystemExit("%s did not converge" % name)
+            if i:
+                times.append(info.Seconds)
+        solves[name] = {"ms": round(statistics.median(times) * 1e3, 3), "iterations": info.NmbIte,
+                        "rel_residual": info.RelRes}
+    G.lib.GmlStop(g)
+    out["cg_96cube"] = {"metric": "FP64 CG time / FP32-CG-in-FP64-IR time", "unit": "x",
+                        "value": round(solves["cg_fp64"]["ms"] / solves["cg_fp32_in_fp64_ir"]["ms"], 3),
+                        "rows": nrow, "blocks": nnzb, "solves": solves}
+    ctypes.CDLL(None).fflush(None)
+    return out
 
 
 # ------------------------------------------------------------- solver workload

@@ -11,8 +11,9 @@ A 4^3-hex Kuhn cube with its boundary triangles referenced by cube side:
   - the flow itself, with this project's statements of the same six bodies
     (tests/kernels/heat_*.cl): the time step within 1e-5, and after 30
     explicit steps the cell values within 1e-4 of their range, the face
-    values likewise, the residual norms within 1e-3 relative (FP32 on both
-    sides; pow and the FMA contractions differ in the last bits)."""
+    values likewise, the residual norms (sums of squares over every cell)
+    within 1e-3 relative (FP32 on both sides; pow and the FMA contractions
+    differ in the last bits)."""
 import ctypes
 import importlib.util
 import os
@@ -127,7 +128,9 @@ def test_heat_cell_centered_flow(G, gpu):
         for k in ks:
             assert G.lib.GmlLaunchKernel(g, k) == 1
         res.append(G.reduce(g, rhs, G.GmlL2))
-    assert np.allclose(res, r["res"], rtol=1e-3, atol=0)
+    # the residual over every line (the reference's own reduction drops the
+    # last partial work-group: r["res"] is kept for the record)
+    assert np.allclose(res, r["res_exact"], rtol=1e-3, atol=0)
     s = G.get_data(g, sol, np.float32, nt)
     span = float(np.ptp(r["sol"])) or 1.0
     assert np.max(np.abs(s - r["sol"])) <= 1e-4 * span
