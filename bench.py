@@ -58,6 +58,9 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=N_HEX, help="hexes per cube side")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--refhost", action="store_true",
+                   help="reference arm: also time the reference's own host library and "
+                        "NodeSmoothing kernels on the CPU (needs the reference tree)")
     p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--workload", default="smooth",
                    choices=["smooth", "quality", "nodesmooth", "solve", "batch", "serve", "p2"],
@@ -289,7 +292,53 @@ def run_reference(args, dist):
             "note": "the reference is OpenCL host code plus OpenCL kernels; no OpenCL "
                     "runtime exists on this box, so its CPU path is the oracle's "
                     "OpenMP port of the same workload"}
+    if args.refhost:
+        line["reference_host_nodesmoothing"] = refhost_nodesmoothing(crd, tet, ref)
     print(json.dumps(line), flush=True)
+
+
+def refhost_nodesmoothing(crd, tet, ref, sweeps=8):
+    """The reference's own NodeSmoothing sweep (examples/NodeSmoothing:
+    scatter, gather with voyeurs, residual sum) through its unmodified host
+    library on the host CPU (oracle/refhost: its generated kernels built by
+    g++, one OpenMP loop over work-items), on the same mesh; seconds per
+    sweep after the reference's work-group calibration (its first 13
+    launches of each kernel).  Only where the reference tree is present."""
+    from oracle import refhost as R
+    from oracle import build as OB
+    if not R.available():
+        return {"unavailable": "the reference tree is not on this machine"}
+    ex = os.path.join(OB.REF_ROOT, "examples", "NodeSmoothing")
+
+    def body(name):
+        with open(os.path.join(ex, name), "rb") as f:
+            return f.read()
+    I = R.Instance()
+    I.parameters(64, body("parameters.cl"))
+    t0 = time.perf_counter()
+    v = I.mesh(R.GmlVertices, crd, ref)
+    I.mesh(R.GmlTetrahedra, tet)
+    o = I.solution(R.GmlTetrahedra, 4, R.GmlFlt4, b"OptCrd")
+    r = I.solution(R.GmlVertices, 1, R.GmlFlt, b"res")
+    ks = I.compile(body("scatter.cl"), b"scatter", R.GmlTetrahedra,
+                   [(v, R.GmlReadMode), (o, R.GmlWriteMode)])
+    kg = I.compile(body("gather.cl"), b"gather", R.GmlVertices,
+                   [(r, R.GmlWriteMode), (o, R.GmlReadMode | R.GmlVoyeurs),
+                    (v, R.GmlReadMode | R.GmlWriteMode)])
+    setup = time.perf_counter() - t0
+    ts = []
+    for i in range(14 + sweeps):
+        t = time.perf_counter()
+        I.launch(ks)
+        I.launch(kg)
+        I.reduce(r, R.GmlSum)
+        if i >= 14:
+            ts.append(time.perf_counter() - t)
+    I.stop()
+    return {"seconds_per_sweep": round(statistics.median(ts), 4), "setup_seconds": round(setup, 2),
+            "threads": R.lib() and __import__("oracle").lib().orc_threads(),
+            "what": "reference host library (ball tables, generated kernels) + its scatter/gather "
+                    "bodies, OpenMP over work-items, g++ -O2"}
 
 
 def working_set(nv, nt, used):

@@ -168,6 +168,9 @@ SIGNATURES.update({
     "GmlxBatchFlags": (_i, [_s, _i, _p, _s]),
     "GmlxBatchTune": (_i, [_s, _i, _f]),
     "GmlxBatchSetTiles": (_i, [_s, _i, _i, _i, _i]),
+    "GmlxSetBallWindow": (_i, [_s, _i]),
+    "GmlxBallWindow": (_i, [_s]),
+    "GmlxMeshTune": (_i, [_s, _i, ctypes.c_float]),
     "GmlxBatchSetWaitLimit": (_i, [_s, _i, _i]),
     "GmlxBatchInfo": (_i, [_s, _ip, _ip, _ip, _ip, _ip]),
     "GmlxServeNew": (_s, [_i, _d, _i]),

@@ -154,6 +154,126 @@ void gmlx_cache_store(const char *src, const char *opts, const char *name, const
 }
 
 /* ========================================================================= */
+/* tuning table (process wide, kept in GML_CACHE_DIR/tune.json when set)      */
+/* ========================================================================= */
+
+/* Choices of the autotuners: the block size of a generated kernel, keyed by
+   its source hash, the binary order of magnitude of its line count and the
+   GPU's SM count ("k:<hash>:<log2 lines>:<sms>"), and the ball-of-points
+   sorting window of a mesh ("w:<log2 vertices>:<sms>").  The file is a
+   JSON object with one "key": value pair per line; it is read once and
+   rewritten after every new choice. */
+typedef struct TuneEnt
+{
+   char key[64];
+   int val;
+   struct TuneEnt *next;
+}TuneEnt;
+
+static TuneEnt *tune_head;
+static int tune_loaded;
+static pthread_mutex_t tune_lock = PTHREAD_MUTEX_INITIALIZER;
+
+static int tune_path(char *buf, size_t n)
+{
+   const char *dir = getenv("GML_CACHE_DIR");
+   if(!dir || !*dir)
+      return 0;
+   snprintf(buf, n, "%s/tune.json", dir);
+   return 1;
+}
+
+static TuneEnt *tune_find(const char *key)
+{
+   for(TuneEnt *e=tune_head;e;e=e->next)
+      if(!strcmp(e->key, key))
+         return e;
+   return NULL;
+}
+
+static void tune_put(const char *key, int val)
+{
+   TuneEnt *e = tune_find(key);
+   if(!e && (e = calloc(1, sizeof(TuneEnt))))
+   {
+      snprintf(e->key, sizeof(e->key), "%s", key);
+      e->next = tune_head;
+      tune_head = e;
+   }
+   if(e)
+      e->val = val;
+}
+
+static void tune_load(void)
+{
+   char path[1024], line[256], key[64];
+   int val;
+   FILE *f;
+   if(tune_loaded)
+      return;
+   tune_loaded = 1;
+   if(!tune_path(path, sizeof(path)) || !(f = fopen(path, "r")))
+      return;
+   while(fgets(line, sizeof(line), f))
+      if(sscanf(line, " \"%63[^\"]\" : %d", key, &val) == 2)
+         tune_put(key, val);
+   fclose(f);
+}
+
+static void tune_save(void)
+{
+   char path[1024], tmp[1100];
+   FILE *f;
+   if(!tune_path(path, sizeof(path)))
+      return;
+   snprintf(tmp, sizeof(tmp), "%s.%d", path, (int)getpid());
+   if(!(f = fopen(tmp, "w")))
+      return;
+   fprintf(f, "{\n");
+   for(TuneEnt *e=tune_head;e;e=e->next)
+      fprintf(f, "\"%s\": %d%s\n", e->key, e->val, e->next ? "," : "");
+   fprintf(f, "}\n");
+   if(fclose(f) == 0)
+      rename(tmp, path);
+   else
+      remove(tmp);
+}
+
+static int log2_floor(long long n)
+{
+   int l = 0;
+   while(n > 1) { n >>= 1; l++; }
+   return l;
+}
+
+int gmlx_tune_get(const char *kind, uint64_t hash, long long count, int nsm)
+{
+   char key[64];
+   TuneEnt *e;
+   int val = 0;
+   snprintf(key, sizeof(key), "%s:%016llx:%d:%d", kind, (unsigned long long)hash,
+            log2_floor(count), nsm);
+   pthread_mutex_lock(&tune_lock);
+   tune_load();
+   if((e = tune_find(key)))
+      val = e->val;
+   pthread_mutex_unlock(&tune_lock);
+   return val;
+}
+
+void gmlx_tune_set(const char *kind, uint64_t hash, long long count, int nsm, int val)
+{
+   char key[64];
+   snprintf(key, sizeof(key), "%s:%016llx:%d:%d", kind, (unsigned long long)hash,
+            log2_floor(count), nsm);
+   pthread_mutex_lock(&tune_lock);
+   tune_load();
+   tune_put(key, val);
+   tune_save();
+   pthread_mutex_unlock(&tune_lock);
+}
+
+/* ========================================================================= */
 /* instance control                                                           */
 /* ========================================================================= */
 

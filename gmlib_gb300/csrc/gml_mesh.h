@@ -18,11 +18,12 @@ int gmd_mesh_vt_csr(struct GmdCtx *ctx, const void *tet, int nt, int nv,
 int gmd_mesh_boundary(struct GmdCtx *ctx, const void *tet, int nt, const int *ptr,
                       const int *vt, int *fixed);
 /* ball of points as SELL-C-sigma: rows are vertices sorted by ball size in
-   windows of 256 (rowv packs (size << 26) | vertex), slices of 32 rows */
+   windows of `window` rows (32, 64, 128 or GML_SIGMA = 256; rowv packs
+   (size << 26) | vertex), slices of 32 rows, rows padded to a multiple of 256 */
 #define GML_SIGMA 256
 int gmd_mesh_point_count(struct GmdCtx *ctx, const void *tet, int nv, const int *ptr,
                          const int *vt, const int *fixed, int *pdeg, unsigned *rowv,
-                         long long *width, long long *soff, int *err);
+                         long long *width, long long *soff, int *err, int window);
 int gmd_mesh_point_fill(struct GmdCtx *ctx, const void *tet, int nrow, const int *ptr,
                         const int *vt, const unsigned *rowv, const long long *soff, int *col);
 /* bps: resident blocks per SM for the persistent grid (0: the kernel's

@@ -158,8 +158,9 @@ __global__ void point_count_kernel(int nv, const int4 *__restrict__ tet, const i
 }
 
 /* SELL-C-sigma layout of the balls of points.  Vertices are sorted by
-   decreasing ball size inside windows of SIGMA consecutive vertices (the
-   Hilbert locality of the numbering is kept), rows are grouped by 32 into
+   decreasing ball size inside windows of sigma consecutive vertices (32 to
+   SIGMA = 256, a tuning choice; the Hilbert locality of the numbering is
+   kept), rows are grouped by 32 into
    slices as wide as their first row, and entry k of the 32 rows of a slice
    is stored contiguously.  rowv[r] packs the vertex of row r and its ball
    size: (d << 26) | v.  One thread per row then streams column indices in
@@ -233,21 +234,23 @@ __device__ __forceinline__ int mbar_wait_bounded(unsigned long long *bar, unsign
    return 0;
 }
 
+/* one block per window of blockDim.x (<= SIGMA) rows: each row's rank in
+   decreasing ball size, ties in vertex order */
 __global__ void __launch_bounds__(SIGMA)
 window_sort_kernel(int nv, const int *__restrict__ pdeg, unsigned *rowv)
 {
    __shared__ int dd[SIGMA];
-   const int t = threadIdx.x, v = blockIdx.x * SIGMA + t;
+   const int w = blockDim.x, t = threadIdx.x, v = blockIdx.x * w + t;
    const int d = v < nv ? pdeg[v] : -1;
    dd[t] = d;
    __syncthreads();
    int rank = 0;
-   for(int u=0;u<SIGMA;u++)
+   for(int u=0;u<w;u++)
    {
       const int du = dd[u];
       rank += (du > d) || (du == d && u < t);
    }
-   rowv[ blockIdx.x * SIGMA + rank ] = v < nv ? (((unsigned)d << ROW_SHIFT) | (unsigned)v) : ROW_NONE;
+   rowv[ blockIdx.x * w + rank ] = v < nv ? (((unsigned)d << ROW_SHIFT) | (unsigned)v) : ROW_NONE;
 }
 
 __global__ void slice_width_kernel(int nslice, const unsigned *__restrict__ rowv, long long *w)
@@ -789,12 +792,14 @@ extern "C" int gmd_mesh_boundary(GmdCtx *ctx, const void *tet, int nt, const int
 
 extern "C" int gmd_mesh_point_count(GmdCtx *ctx, const void *tet, int nv, const int *ptr,
                                     const int *vt, const int *fixed, int *pdeg, unsigned *rowv,
-                                    long long *width, long long *soff, int *err)
+                                    long long *width, long long *soff, int *err, int window)
 {
    cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
-   const int nwin = (nv + SIGMA - 1) / SIGMA, nslice = nwin * (SIGMA / 32);
+   const int nrow = (nv + SIGMA - 1) / SIGMA * SIGMA, nslice = nrow / 32;
+   if(window < 32 || window > SIGMA || SIGMA % window)
+      return 0;
    point_count_kernel<<<nblk(nv, 128), 128, 0, st>>>(nv, (const int4 *)tet, ptr, vt, fixed, pdeg, err);
-   window_sort_kernel<<<nwin, SIGMA, 0, st>>>(nv, pdeg, rowv);
+   window_sort_kernel<<<nrow / window, window, 0, st>>>(nv, pdeg, rowv);
    slice_width_kernel<<<nblk(nslice, MK_THREADS), MK_THREADS, 0, st>>>(nslice, rowv, width);
    if(!gmd_scan_excl_i64(ctx, width, soff, nslice))
       return 0;

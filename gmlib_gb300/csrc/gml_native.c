@@ -23,6 +23,9 @@
 #define GML_SPLIT_L 3
 #endif
 
+static int ready(GmlSct *gml, NatSct **n, GmlDatSct **ver, GmlDatSct **tet);
+static int sweeps(GmlSct *gml, NatSct *n, GmlDatSct *ver, int ns, float omega);
+
 NatSct *gmlx_nat(GmlSct *gml)
 {
    if(!gml->ext)
@@ -83,7 +86,11 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
       return 0;
 
    n = gmlx_nat(gml);
-   free_state(gml, n);
+   {
+      const int wreq = n->wreq;
+      free_state(gml, n);
+      n->wreq = wreq;
+   }
    nv = ver->NmbLin;
    nt = tet->NmbLin;
    if(nv >= (1 << 26))
@@ -93,6 +100,9 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
    }
    n->nv = nv;
    n->nrow = ((nv + GML_SIGMA - 1) / GML_SIGMA) * GML_SIGMA;
+   n->window = n->wreq ? n->wreq : gmlx_tune_get("w", 0, nv, gmd_num_sms(gml->dev));
+   if(n->window != 32 && n->window != 64 && n->window != 128 && n->window != GML_SIGMA)
+      n->window = GML_SIGMA;
    nslice = n->nrow / 32;
    n->nt = nt;
    n->fix = fix;
@@ -142,8 +152,12 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
       gmd_mesh_boundary(gml->dev, tet->GpuMem, nt, n->ptr, n->vt, n->fixed);
    }
 
-   gmd_mesh_point_count(gml->dev, tet->GpuMem, nv, n->ptr, n->vt, n->fixed, n->pdeg,
-                        n->rowv, n->width, n->soff, n->err);
+   if(!gmd_mesh_point_count(gml->dev, tet->GpuMem, nv, n->ptr, n->vt, n->fixed, n->pdeg,
+                            n->rowv, n->width, n->soff, n->err, n->window))
+   {
+      free_state(gml, n);
+      return 0;
+   }
 
    pdeg_h = malloc((size_t)nv * sizeof(int));
    if(!pdeg_h)
@@ -184,6 +198,77 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
    gmd_sync(gml->dev);
    n->ready = 1;
    return 1;
+}
+
+int GmlxSetBallWindow(size_t GmlIdx, int window)
+{
+   GETGMLPTR(gml, GmlIdx);
+   NatSct *n;
+   if(window && window != 32 && window != 64 && window != 128 && window != GML_SIGMA)
+      return 0;
+   if(!(n = gmlx_nat(gml)))
+      return 0;
+   n->wreq = window;
+   return 1;
+}
+
+int GmlxBallWindow(size_t GmlIdx)
+{
+   GETGMLPTR(gml, GmlIdx);
+   NatSct *n = gml->ext;
+   return n && n->ready ? n->window : 0;
+}
+
+/* Time nsweeps sweeps with each sorting window on the current mesh (rebuilt
+   by GmlxMeshSetup with the fixing rule in force), keep the fastest, record
+   it in the tuning table for meshes of this size, and leave the mesh built
+   with it; the coordinates are restored. */
+int GmlxMeshTune(size_t GmlIdx, int nsweeps, float omega)
+{
+   static const int cand[] = { 64, 128, GML_SIGMA };
+   GETGMLPTR(gml, GmlIdx);
+   NatSct *n;
+   GmlDatSct *ver, *tet;
+   void *save, *e0, *e1;
+   double best_t = 1e30;
+   int best = GML_SIGMA, fix;
+
+   if(!ready(gml, &n, &ver, &tet) || nsweeps < 1)
+      return 0;
+   fix = n->fix;
+   if(!(save = gmd_alloc(gml->dev, (size_t)n->nv * 16)))
+      return 0;
+   e0 = gmd_event_new();
+   e1 = gmd_event_new();
+   gmd_d2d_async(gml->dev, save, ver->GpuMem, (size_t)n->nv * 16);
+   for(int c=0;c<(int)(sizeof(cand) / sizeof(cand[0]));c++)
+   {
+      double t;
+      n->wreq = cand[c];
+      if(!GmlxMeshSetup(GmlIdx, fix) || !sweeps(gml, n, ver, 1, omega))
+         break;
+      gmd_event_record(gml->dev, e0);
+      if(!sweeps(gml, n, ver, nsweeps, omega))
+         break;
+      gmd_event_record(gml->dev, e1);
+      t = gmd_event_elapsed_s(e0, e1);
+      gmd_d2d_async(gml->dev, ver->GpuMem, save, (size_t)n->nv * 16);
+      if(t > 0. && t < best_t)
+      {
+         best_t = t;
+         best = cand[c];
+      }
+   }
+   gmd_d2d_async(gml->dev, ver->GpuMem, save, (size_t)n->nv * 16);
+   gmd_sync(gml->dev);
+   gmd_free(gml->dev, save);
+   gmd_event_free(e0);
+   gmd_event_free(e1);
+   gmlx_tune_set("w", 0, n->nv, gmd_num_sms(gml->dev), best);
+   n->wreq = best;
+   if(!GmlxMeshSetup(GmlIdx, fix))
+      return 0;
+   return best;
 }
 
 int GmlxMeshBallInfo(size_t GmlIdx, long long *stored, long long *used, int *maxdeg)

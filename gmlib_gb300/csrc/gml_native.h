@@ -15,7 +15,9 @@
 typedef struct
 {
    int         nv, nt, fix, ready;
-   int         nrow;                  /* rows of the SELL layout (windows x 256) */
+   int         nrow;                  /* rows of the SELL layout (a multiple of 256) */
+   int         window;                /* rows sorted by ball size together (32..256) */
+   int         wreq;                  /* window asked for by GmlxSetBallWindow, 0: auto */
    int         *ptr, *vt, *tmp, *err, *fixed, *pdeg, *pcol;
    unsigned    *rowv;
    long long   *width, *soff;

@@ -909,14 +909,23 @@ int gml_timed_launch(GmlSct *gml, GmlKrnSct *krn, unsigned grid, unsigned block,
 
 static const int TunCand[] = { 64, 128, 256, 512, 1024, 32 };
 #define NMB_TUNCAND ((int)(sizeof(TunCand) / sizeof(TunCand[0])))
+#define NMB_TUNRND  2            /* timings of each candidate; the fastest counts */
 
 /* Block-size calibration.  Like the reference (:3142-3190) the first launches
    of a kernel try several work-group sizes and keep the fastest; here the
    candidates are warp multiples timed with CUDA events instead of a host
-   clock around clFinish, and the choice is made once all candidates ran. */
+   clock around clFinish: launch 0 warms up with 256, launches 1 to
+   NMB_TUNRND x NMB_TUNCAND time the candidates in turn, each NMB_TUNRND
+   times (a kernel's launches do the caller's work, so the rounds are spread
+   over its first launches), and each candidate's best time counts.  The
+   choice is kept in the process-wide tuning table under the kernel's source
+   hash, line count and SM count, and persisted when GML_CACHE_DIR is set:
+   a later kernel with the same key starts with the choice. */
 static int pick_block(GmlSct *gml, GmlKrnSct *krn)
 {
-   int lim = krn->MaxSiz > 0 ? krn->MaxSiz : 1024, c, best = -1;
+   const int lim = krn->MaxSiz > 0 ? krn->MaxSiz : 1024;
+   const int nstep = NMB_TUNRND * NMB_TUNCAND;
+   int c, best = -1;
    double tbest = 1e30;
 
    if(krn->OptSiz)
@@ -929,10 +938,16 @@ static int pick_block(GmlSct *gml, GmlKrnSct *krn)
       return krn->OptSiz;
    }
 
-   /* step 0 warms up, steps 1..NMB_TUNCAND time one candidate each */
-   if(krn->TunStp <= NMB_TUNCAND)
+   if(krn->TunStp == 0)
    {
-      c = krn->TunStp == 0 ? 2 : krn->TunStp - 1;
+      const int known = gmlx_tune_get("k", krn->hash, krn->NmbLin[0], gmd_num_sms(gml->dev));
+      if(known >= 32 && known <= lim)
+         return krn->OptSiz = known;
+   }
+
+   if(krn->TunStp <= nstep)
+   {
+      c = krn->TunStp == 0 ? 2 : (krn->TunStp - 1) % NMB_TUNCAND;
       krn->TunStp++;
       while(TunCand[c] > lim && c > 0)
          c--;
@@ -947,6 +962,8 @@ static int pick_block(GmlSct *gml, GmlKrnSct *krn)
       }
 
    krn->OptSiz = best > 0 ? best : (lim < 256 ? lim : 256);
+   if(best > 0)
+      gmlx_tune_set("k", krn->hash, krn->NmbLin[0], gmd_num_sms(gml->dev), krn->OptSiz);
    return krn->OptSiz;
 }
 
@@ -983,15 +1000,19 @@ static int run_generated(GmlSct *gml, GmlKrnSct *krn)
    blk = pick_block(gml, krn);
    grid = (unsigned)((cnt[0] + blk - 1) / blk);
 
-   if(tuning && step >= 1 && step <= NMB_TUNCAND && krn->OptSiz == 0)
+   if(tuning && step >= 1 && step <= NMB_TUNRND * NMB_TUNCAND && krn->OptSiz == 0)
    {
-      int c = step - 1, res;
+      const int c = (step - 1) % NMB_TUNCAND;
+      int res;
+      double t;
       if(!krn->TunBeg) krn->TunBeg = gmd_event_new();
       if(!krn->TunEnd) krn->TunEnd = gmd_event_new();
       gmd_event_record(gml->dev, krn->TunBeg);
       res = gml_timed_launch(gml, krn, grid, (unsigned)blk, args);
       gmd_event_record(gml->dev, krn->TunEnd);
-      krn->TunTim[c] = TunCand[c] == blk ? gmd_event_elapsed_s(krn->TunBeg, krn->TunEnd) : 0.;
+      t = TunCand[c] == blk ? gmd_event_elapsed_s(krn->TunBeg, krn->TunEnd) : 0.;
+      if(t > 0. && (krn->TunTim[c] <= 0. || t < krn->TunTim[c]))
+         krn->TunTim[c] = t;
       return res ? 1 : -6;
    }
 
@@ -1115,6 +1136,7 @@ static int compile_into_slot(GmlSct *gml, const char *src, const char *PrcNam, i
       if(!(idx = gml_new_kernel_slot(gml, GmlKrnGenerated, PrcNam)))
          return 0;
       gml->krn[ idx ].source = strdup(src);
+      gml->krn[ idx ].hash = gml_hash64(src, strlen(src), 0x9e3779b97f4a7c15ULL);
       return idx;
    }
 
@@ -1137,6 +1159,7 @@ static int compile_into_slot(GmlSct *gml, const char *src, const char *PrcNam, i
    gml->krn[ idx ].MaxSiz = maxthr;
    gml->krn[ idx ].NumReg = nreg;
    gml->krn[ idx ].source = strdup(src);
+   gml->krn[ idx ].hash = gml_hash64(src, strlen(src), 0x9e3779b97f4a7c15ULL);
    return idx;
 }
 

@@ -201,6 +201,19 @@ int      GmlxMeshSetup        (size_t, int fix);
    used (sum of degrees). */
 int      GmlxMeshBallInfo     (size_t, long long *stored, long long *used, int *maxdeg);
 
+/* The ball-of-points layout sorts rows by ball size inside windows of 32,
+   64, 128 or 256 consecutive vertices: wider windows pad less, narrower ones
+   keep rows nearer their Hilbert neighbours.  GmlxSetBallWindow fixes the
+   window of the next GmlxMeshSetup (0: the tuning table's choice for meshes
+   of that size, else 256); GmlxBallWindow returns the window in use.
+   GmlxMeshTune times nsweeps sweeps with each window on the current mesh,
+   keeps the fastest (rebuilding the layout; coordinates restored), records
+   it in the tuning table and returns it (0 on error).  The results do not
+   depend on the window. */
+int      GmlxSetBallWindow    (size_t, int window);
+int      GmlxBallWindow       (size_t);
+int      GmlxMeshTune         (size_t, int nsweeps, float omega);
+
 /* nsweeps Jacobi sweeps x <- x + omega (mean of the ball of points - x) of
    the vertex coordinates, in place; fixed vertices do not move. */
 int      GmlxSmooth           (size_t, int nsweeps, float omega);
@@ -447,6 +460,8 @@ int      gmlx_cache_lookup(const char *src, const char *opts, const char *name, 
 void     gmlx_cache_store(const char *src, const char *opts, const char *name, const void *cubin, size_t size);
 int      gmlx_timing_off(GmlSct *gml);
 void     gmlx_release_extensions(GmlSct *gml);
+int      gmlx_tune_get(const char *kind, uint64_t hash, long long count, int nsm);
+void     gmlx_tune_set(const char *kind, uint64_t hash, long long count, int nsm, int val);
 #endif
 
 #endif

@@ -5,6 +5,7 @@ tables."""
 import ctypes
 import os
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -296,7 +297,7 @@ def test_kernel_timing_and_calibration(G, gpu):
     k = G.compile_kernel(gpu, body("tet_quality.cl"), "quality", G.GmlTetrahedra,
                          [(v, G.GmlReadMode, 0), (q, G.GmlWriteMode, 0)])
     first = None
-    for i in range(10):
+    for i in range(1 + 2 * 6 + 2):            # warm-up, 2 timings of 6 candidates, choice
         assert G.lib.GmlLaunchKernel(gpu, k) == 1
         if i == 0:
             first = G.get_data(gpu, q, np.float32, len(tet))
@@ -306,3 +307,43 @@ def test_kernel_timing_and_calibration(G, gpu):
     assert G.lib.GmlGetKernelRunTime(gpu, k) > 0
     G.reduce(gpu, q, G.GmlSum)
     assert G.lib.GmlGetReduceRunTime(gpu, G.GmlSum) > 0
+
+
+TUNE_SCRIPT = r"""
+import sys, numpy as np
+sys.path.insert(0, %r)
+sys.path.insert(0, %r)
+import gmlib_gb300 as G
+from conftest import PARAMS
+crd, tet, ref = G.cube_mesh(40, split=0, jitter=0.25, seed=5)
+g = G.lib.GmlInit(0)
+G.lib.GmlNewParameters(g, 8, PARAMS)
+v, t = G.upload_mesh(g, crd, tet, ref)
+q = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 1, G.GmlFlt, b"qal")
+src = open(%r, "rb").read()
+k = G.compile_kernel(g, src, "quality", G.GmlTetrahedra, [(v, G.GmlReadMode, 0), (q, G.GmlWriteMode, 0)])
+n = int(sys.argv[1])
+for _ in range(n):
+    assert G.lib.GmlLaunchKernel(g, k) == 1
+print(G.lib.GmlxKernelBlockSize(g, k))
+G.lib.GmlStop(g)
+"""
+
+
+def test_calibration_is_kept_in_the_tuning_file(tmp_path):
+    """A process that calibrated a kernel writes its block size to
+    GML_CACHE_DIR/tune.json; a later process compiling the same kernel on
+    the same line count starts with that block size (no calibration)."""
+    script = TUNE_SCRIPT % (ROOT, os.path.join(ROOT, "tests"), os.path.join(KDIR, "tet_quality.cl"))
+    env = dict(os.environ, GML_CACHE_DIR=str(tmp_path))
+    first = subprocess.run([sys.executable, "-c", script, "15"], env=env, capture_output=True,
+                           text=True, timeout=300)
+    assert first.returncode == 0, first.stderr
+    chosen = int(first.stdout.split()[-1])
+    assert chosen in (32, 64, 128, 256, 512, 1024)
+    text = (tmp_path / "tune.json").read_text()
+    assert text.startswith("{") and '"k:' in text and (": %d" % chosen) in text
+    again = subprocess.run([sys.executable, "-c", script, "1"], env=env, capture_output=True,
+                           text=True, timeout=300)
+    assert again.returncode == 0, again.stderr
+    assert int(again.stdout.split()[-1]) == chosen

@@ -106,3 +106,29 @@ def test_smoothing_loop_graph_matches_oracle(G, O, gpu):
     got2 = G.get_data(gpu, v, np.float32, (len(crd), 4))
     exp2 = O.laplace(got.astype(np.float64), ptr, col, 1.0, 10)
     assert np.max(np.abs(got2 - exp2)) <= 1e-5
+
+
+def test_ball_window_tuning_keeps_results(G, O, gpu):
+    """The sorting window of the ball-of-points layout changes the padding,
+    not the results: sweeps with windows 64 and 256 are bit-identical, and
+    GmlxMeshTune picks a window, leaves the coordinates untouched and
+    records the window in use."""
+    n = 24
+    crd, tet, ref = G.cube_mesh(n, split=1, jitter=0.3, seed=9)
+    v, t = G.upload_mesh(gpu, crd, tet, ref)
+    out = {}
+    for w in (64, 256):
+        assert G.lib.GmlxSetBallWindow(gpu, w) == 1
+        assert G.lib.GmlxMeshSetup(gpu, 1) == 1
+        assert G.lib.GmlxBallWindow(gpu) == w
+        G.set_data(gpu, v, crd)
+        assert G.lib.GmlxSmooth(gpu, 3, ctypes.c_float(0.7)) == 1
+        out[w] = G.get_data(gpu, v, np.float32, (len(crd), 4))
+    assert np.array_equal(out[64], out[256])
+    ptr, col = O.point_ball(len(crd), tet, (ref != 0).astype(np.int32))
+    assert np.max(np.abs(out[64] - O.laplace(crd, ptr, col, 0.7, 3))) <= 2e-6
+    G.set_data(gpu, v, crd)
+    w = G.lib.GmlxMeshTune(gpu, 3, ctypes.c_float(0.7))
+    assert w in (64, 128, 256) and G.lib.GmlxBallWindow(gpu) == w
+    assert np.array_equal(G.get_data(gpu, v, np.float32, (len(crd), 4)), crd)
+    assert G.lib.GmlxSetBallWindow(gpu, 100) == 0
