@@ -58,6 +58,9 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=N_HEX, help="hexes per cube side")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-other-configs", action="store_true",
+                   help="smooth: leave out the compact results of the quality, solver and "
+                        "batch configurations (for profiler runs of the step alone)")
     p.add_argument("--refhost", action="store_true",
                    help="reference arm: also time the reference's own host library and "
                         "NodeSmoothing kernels on the CPU (needs the reference tree)")
@@ -471,7 +474,7 @@ def run_gpu(args, dist):
                               and abs(first.MinQal - port["min"]) <= 2e-5
                               and first.NmbInv == port["inverted"])}
 
-    others = other_configs(G, dev) if dist.world == 1 else None
+    others = other_configs(G, dev) if dist.world == 1 and not args.no_other_configs else None
 
     G.lib.GmlStop(g)
 
@@ -497,9 +500,10 @@ def run_gpu(args, dist):
 def other_configs(G, dev):
     """Compact results of the plain-quality configuration (32^3-hex Kuhn
     cube, 196,608 tets: one quality pass with statistics, L2 flushed before
-    each of 20 launches) and of the solver configuration (96^3-hex SPD
+    each of 20 launches), of the solver configuration (96^3-hex SPD
     block system: FP64 CG and FP32 CG inside FP64 refinement to 1e-10,
-    median of 3 solves after one), for the default run."""
+    median of 3 solves after one) and of the batch configuration (512
+    meshes, 5 runs of each path after 2), for the default run."""
     out = {}
     n = Q_N
     crd, tet, ref = G.cube_mesh(n, split=0, jitter=Q_JITTER, seed=Q_SEED)
@@ -554,6 +558,12 @@ def other_configs(G, dev):
     out["cg_96cube"] = {"metric": "FP64 CG time / FP32-CG-in-FP64-IR time", "unit": "x",
                         "value": round(solves["cg_fp64"]["ms"] / solves["cg_fp32_in_fp64_ir"]["ms"], 3),
                         "rows": nrow, "blocks": nnzb, "solves": solves}
+    bo, bi = batch_measure(G, dev, 512, 5, 2)
+    out["batch_512meshes"] = {"metric": "batched meshes/s (5 sweeps + quality + min per mesh)",
+                              "unit": "meshes/s", "value": bo["queue"]["meshes_per_s"],
+                              "queue": bo["queue"], "loop": bo["loop"],
+                              "speedup_vs_loop": bi["speedup_vs_loop"], "tets": bi["tets"],
+                              "frac": bi["roofline"]["frac"], "min_quality": bi["min_quality"]}
     ctypes.CDLL(None).fflush(None)
     return out
 
@@ -1086,14 +1096,14 @@ def run_p2(args, dist):
         print(json.dumps(line), flush=True)
 
 
-def run_batch(args, dist):
-    """512 jittered tet cubes, hexes per side log-uniform in [10, 80], reflected
-    split, Hilbert order: 5 sweeps + quality statistics (min/argmin) per mesh,
-    through one persistent tile-queue launch (CUDA graph, tuned tiles) and
-    through the per-mesh launch loop.  meshes/s over --steps runs of each."""
-    import gmlib_gb300 as G
+def batch_measure(G, dev, nmesh, steps, warmup):
+    """Config-4 batch: nmesh jittered tet cubes, hexes per side log-uniform in
+    [10, 80], reflected split, Hilbert order; 5 sweeps + quality statistics
+    (min/argmin) per mesh, through one persistent tile-queue launch (CUDA
+    graph, tuned tiles) and through the per-mesh launch loop, `steps` runs of
+    each after `warmup`."""
     rng = np.random.default_rng(SEED)
-    ns = np.exp(rng.uniform(np.log(10), np.log(80), args.meshes)).astype(int)
+    ns = np.exp(rng.uniform(np.log(10), np.log(80), nmesh)).astype(int)
     t0 = time.time()
     ms = gen_meshes([(int(n), 1, 0.3, SEED + i) for i, n in enumerate(ns)])
     tgen = time.time() - t0
@@ -1101,64 +1111,80 @@ def run_batch(args, dist):
     nt = np.array([len(m[1]) for m in ms], np.int32)
     degrees = degree_summary([m[1] for m in ms])
     h = 1.0 / ns.astype(np.float64)
-    g = G.lib.GmlInit(dist.local)
+    g = G.lib.GmlInit(dev)
     G.lib.GmlxSetTiming(g, 0)
     if G.lib.GmlxBatchCreate(g, len(ms), G.as_ptr(nv), G.as_ptr(nt), G.as_ptr(h)) != 1:
         raise SystemExit("GmlxBatchCreate failed")
     for i, (crd, tet, ref) in enumerate(ms):
         G.lib.GmlxBatchSetMesh(g, i, G.as_ptr(crd), G.as_ptr(ref), G.as_ptr(tet))
+    del ms
     if G.lib.GmlxBatchSetup(g, 1) != 1:
         raise SystemExit("GmlxBatchSetup failed")
     sweeps, om = 5, ctypes.c_float(OMEGA)
     G.lib.GmlxBatchTune(g, sweeps, om)
     ts_, tt_, gr_, ntile, wt_ = (ctypes.c_int() for _ in range(5))
-    res = (G.GmlxQuality * len(ms))()
+    res = (G.GmlxQuality * nmesh)()
     e0, e1 = G.lib.GmlxEventCreate(), G.lib.GmlxEventCreate()
     out = {}
-    clocks = Clocks(dist.local)
+    clocks = Clocks(dev)
     clocks.start()
     for name, mode in (("queue", G.GmlxBatchQueue), ("loop", G.GmlxBatchLoop)):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             G.lib.GmlxBatchRun(g, sweeps, om, mode, None)
         G.lib.GmlxSynchronize(g)
         G.lib.GmlxEventRecord(g, e0)
-        for _ in range(args.steps):
+        for _ in range(steps):
             if G.lib.GmlxBatchRun(g, sweeps, om, mode, None) != 1:
                 raise SystemExit("GmlxBatchRun failed")
         G.lib.GmlxEventRecord(g, e1)
-        t = G.lib.GmlxEventElapsed(e0, e1) / args.steps
-        out[name] = {"ms_per_run": round(t * 1e3, 3), "meshes_per_s": round(len(ms) / t, 1)}
+        t = G.lib.GmlxEventElapsed(e0, e1) / steps
+        out[name] = {"ms_per_run": round(t * 1e3, 3), "meshes_per_s": round(nmesh / t, 1)}
     clk = clocks.stop()
     G.lib.GmlxBatchRun(g, sweeps, om, G.GmlxBatchQueue, res)
     G.lib.GmlxBatchInfo(g, ctypes.byref(ts_), ctypes.byref(tt_), ctypes.byref(gr_),
                         ctypes.byref(ntile), ctypes.byref(wt_))
     stored, used, mx = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
     G.lib.GmlxMeshBallInfo(g, ctypes.byref(stored), ctypes.byref(used), ctypes.byref(mx))
+    G.lib.GmlxEventDestroy(e0)
+    G.lib.GmlxEventDestroy(e1)
+    G.lib.GmlStop(g)
     vpad = float(sum((int(v) + 255) // 256 * 256 for v in nv))
     byts = sweeps * (36.0 * vpad + 4.0 * used.value) + 16.0 * nt.sum() + 16.0 * vpad \
         + 4.0 * sum((int(t) + 31) // 32 for t in nt)
-    G.lib.GmlStop(g)
     peak, _ = peak_hbm()
     tq = out["queue"]["ms_per_run"] / 1e3
+    info = {"tets": int(nt.sum()), "vertices": int(nv.sum()), "sweeps": sweeps,
+            "degrees": degrees, "generation_s": round(tgen, 1),
+            "speedup_vs_loop": round(out["loop"]["ms_per_run"] / out["queue"]["ms_per_run"], 2),
+            "tiles": {"claimed_per": "warp" if wt_.value else "block",
+                      "slices_per_sweep_tile": ts_.value, "tets_per_quality_tile": tt_.value,
+                      "grid": gr_.value, "tiles": ntile.value},
+            "roofline": {"bound": "hbm", "algorithmic_bytes_per_run": byts,
+                         "achieved": round(byts / tq / 1e9, 1), "peak": peak,
+                         "frac": round(byts / tq / 1e9 / peak, 4), "unit": "GB/s"},
+            "min_quality": float(min(r.MinQal for r in res)), "clocks": clk}
+    return out, info
+
+
+def run_batch(args, dist):
+    """The batch configuration (batch_measure) as the bench line, meshes/s
+    over --steps runs of each path."""
+    import gmlib_gb300 as G
+    out, info = batch_measure(G, dist.local, args.meshes, args.steps, args.warmup)
     if dist.rank == 0:
         line = {"metric": "batched meshes/s (5 sweeps + quality + min per mesh)",
                 "value": out["queue"]["meshes_per_s"], "unit": "meshes/s", "n_gpus": dist.world,
                 "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                 "dtype": "f32", "data": "synthetic",
                 "config": {"workload": "%d jittered tet cubes, hexes per side log-uniform in "
-                                       "[10, 80], reflected split" % len(ms),
-                           "tets": int(nt.sum()), "vertices": int(nv.sum()), "sweeps": sweeps,
-                           "vertex_tet_degrees": degrees,
-                           "generation_s": round(tgen, 1)},
+                                       "[10, 80], reflected split" % args.meshes,
+                           "tets": info["tets"], "vertices": info["vertices"],
+                           "sweeps": info["sweeps"], "vertex_tet_degrees": info["degrees"],
+                           "generation_s": info["generation_s"]},
                 "queue": out["queue"], "loop": out["loop"],
-                "speedup_vs_loop": round(out["loop"]["ms_per_run"] / out["queue"]["ms_per_run"], 2),
-                "tiles": {"claimed_per": "warp" if wt_.value else "block",
-                          "slices_per_sweep_tile": ts_.value, "tets_per_quality_tile": tt_.value,
-                          "grid": gr_.value, "tiles": ntile.value},
-                "roofline": {"bound": "hbm", "algorithmic_bytes_per_run": byts,
-                             "achieved": round(byts / tq / 1e9, 1), "peak": peak,
-                             "frac": round(byts / tq / 1e9 / peak, 4), "unit": "GB/s"},
-                "min_quality": float(min(r.MinQal for r in res)), "clocks": clk}
+                "speedup_vs_loop": info["speedup_vs_loop"], "tiles": info["tiles"],
+                "roofline": info["roofline"], "min_quality": info["min_quality"],
+                "clocks": info["clocks"]}
         print(json.dumps(line), flush=True)
 
 
