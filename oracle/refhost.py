@@ -149,6 +149,17 @@ class Instance:
         ok = self.L.GmlGetLinkInfo(self.g, src, dst, *[ctypes.byref(x) for x in v])
         return (ok,) + tuple(x.value for x in v)
 
+    def set_lines(self, idx, rows):
+        """GmlSetDataLine over every line of a raw (solution) datatype: row i
+        of `rows` (any dtype, one line's bytes) is passed by address."""
+        a = np.ascontiguousarray(rows)
+        step = a.strides[0]
+        for i in range(len(a)):
+            r = self.L.GmlSetDataLine(ctypes.c_size_t(self.g), ctypes.c_int(idx), ctypes.c_int(i),
+                                      ctypes.c_void_p(a.ctypes.data + i * step))
+            if r != 1:
+                raise RuntimeError("reference GmlSetDataLine returned %d" % r)
+
     def get_lines(self, idx, n, fmt):
         """GmlGetDataLine over lines 0..n-1 (line 0 downloads the buffer).
         fmt: 'ii' for (int, int, ref), 'iii', 'iiii' ..., 'ddd' for vertices."""
@@ -165,13 +176,17 @@ class Instance:
 
     # ---- kernels ---------------------------------------------------------------
     def compile(self, src, name, msh, dats):
-        """dats: (data index, flags) pairs, link index NULL as in the examples."""
+        """dats: (data index, flags) pairs, or (data index, flags, link
+        index) triplets; the link index is 0 (NULL in the examples) unless
+        given.  The reference reads all three as ints (gmlib3.c:2238-2244)."""
         s = ctypes.create_string_buffer(src)
         nm = ctypes.create_string_buffer(name)
         self._keep += [s, nm]
         args = []
-        for d, f in dats:
-            args += [ctypes.c_int(d), ctypes.c_int(f), ctypes.c_void_p(0)]
+        for item in dats:
+            d, f = item[0], item[1]
+            lk = item[2] if len(item) > 2 else 0
+            args += [ctypes.c_int(d), ctypes.c_int(f), ctypes.c_int(lk)]
         k = self.L.GmlCompileKernel(ctypes.c_size_t(self.g), s, nm, ctypes.c_int(msh),
                                     ctypes.c_int(len(dats)), *args)
         if k <= 0:

@@ -46,6 +46,16 @@ produced:
                    4^3-hex Kuhn cube with side-referenced boundary triangles:
                    faces, triangle -> tet shells, tet -> triangle links, the
                    time step, 30 explicit steps (see make_heat)
+  refhost_examples.npz   the GpuBandwidth, TestFeatures and BallQuality
+                   flows with their own bodies (see make_examples): on the
+                   5^3-hex Kuhn cube the direct, downlink and ball kernels'
+                   outputs, and three TestFeatures iterations (tet and
+                   vertex fields, residual sums as returned and over every
+                   line); on a 12 x 12 jittered square of triangles the
+                   triangle qualities and their vertex-ball minima.  The
+                   example's neighbours kernel is left out: it writes
+                   nothing, and the reference's neighbour link holds pointer
+                   bits (gmlib3.c:4258), so its reads would leave the arrays
 
 Usage:  python tests/golden/make_refhost.py        (needs the reference tree)
 """
@@ -457,12 +467,137 @@ def make_heat():
     I.stop()
 
 
+EX_ITERS = 3
+
+
+def examples_mesh():
+    import gmlib_gb300 as G
+    return G.cube_mesh(5, split=0, jitter=0.2, seed=31)
+
+
+def square_mesh(n=12, jitter=0.3, seed=8):
+    """A jittered n x n square of the z = 0 plane, each cell split into two
+    triangles; interior vertices move by up to jitter * h in x and y."""
+    rng = np.random.default_rng(seed)
+    i, j = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    i, j = i.ravel(), j.ravel()
+    crd = np.zeros((len(i), 4), np.float32)
+    crd[:, 0], crd[:, 1] = i / n, j / n
+    inner = (i > 0) & (i < n) & (j > 0) & (j < n)
+    crd[inner, :2] += rng.uniform(-jitter / n, jitter / n, (int(inner.sum()), 2)).astype(np.float32)
+    tri = []
+    for a in range(n):
+        for b in range(n):
+            p, q, r, s = a * (n + 1) + b, (a + 1) * (n + 1) + b, (a + 1) * (n + 1) + b + 1, a * (n + 1) + b + 1
+            tri += [(p, q, r), (p, r, s)]
+    return crd, np.array(tri, np.int32)
+
+
+def make_examples():
+    """Three more example flows, with the examples' own bodies, on small
+    meshes (the 5^3-hex Kuhn cube, and a 12 x 12 jittered square of
+    triangles): GpuBandwidth (gpu_bandwidth.c:100-175), TestFeatures
+    (TestFeatures.c:95-215, EX_ITERS iterations with GmlPar->res = i) and
+    BallQuality (BallQuality.c:73-130)."""
+    crd, tet, ref = examples_mesh()
+    nv, nt = len(crd), len(tet)
+    out = dict(crd=crd, tet=tet, ref=ref)
+    Rd, Wr = R.GmlReadMode, R.GmlWriteMode
+
+    # GpuBandwidth: the four kernels in the example's order
+    I = R.Instance()
+    I.parameters(8, body("GpuBandwidth/parameters.cl"))
+    v = I.mesh(R.GmlVertices, crd, ref)
+    t = I.mesh(R.GmlTetrahedra, tet)
+    vd = I.solution(R.GmlVertices, 1, R.GmlFlt4, b"VerDat")
+    td = I.solution(R.GmlTetrahedra, 1, R.GmlFlt4, b"TetDat")
+    first = R.lib().refhost_nkernels()
+    ks = [I.compile(body("GpuBandwidth/direct_vertices.cl"), b"direct_vertices", R.GmlVertices,
+                    [(v, Rd), (vd, Wr)]),
+          I.compile(body("GpuBandwidth/direct_tets.cl"), b"direct_tets", R.GmlTetrahedra,
+                    [(t, Rd), (td, Wr)]),
+          I.compile(body("GpuBandwidth/indirect_tets.cl"), b"indirect_tets", R.GmlTetrahedra,
+                    [(v, Rd), (td, Wr)]),
+          I.compile(body("GpuBandwidth/vertices_ball.cl"), b"vertices_ball", R.GmlVertices,
+                    [(vd, Wr), (td, Rd)])]
+    names = ["direct_vertices", "direct_tets", "indirect_tets", "vertices_ball"]
+    obj = {n: [k for k in R.kernel_objects(n) if k >= first][0] for n in names}
+    ok, n, w, N, W = I.link_info(R.GmlVertices, R.GmlTetrahedra)
+    assert ok == 1 and N == 0, "the ball fits the base table"
+    for k, nm, key, dat, shape in zip(ks, names, ["bw_ver", "bw_tet_nodes", "bw_tet_sum", "bw_ball"],
+                                      ["VerDatTab", "TetDatTab", "TetDatTab", "VerDatTab"],
+                                      [(nv, 4), (nt, 4), (nt, 4), (nv, 4)]):
+        I.launch(k)
+        out[key] = f32(R.kernel_buffers(obj[nm])[dat], shape)
+    I.stop()
+
+    # TestFeatures: neighbours (left out below), the FP64 kernel, downlink,
+    # uplink and the residual sum, EX_ITERS times
+    I = R.Instance()
+    p = I.parameters(8, body("TestFeatures/parameters.cl"))
+    v = I.mesh(R.GmlVertices, crd, ref)
+    I.mesh(R.GmlTetrahedra, tet)
+    sol = I.solution(R.GmlVertices, 2, R.GmlFlt4, b"SolAtVer")
+    I.set_lines(sol, np.full((nv, 8), 0.125, np.float32))
+    mid = I.solution(R.GmlTetrahedra, 1, R.GmlFlt4, b"TetMid")
+    res = I.solution(R.GmlTetrahedra, 1, R.GmlFlt, b"ResVec")
+    f64 = I.solution(R.GmlTetrahedra, 1, R.GmlDbl, b"F64Dat")
+    first = R.lib().refhost_nkernels()
+    kf = I.compile(body("TestFeatures/double_precision.cl"), b"double_precision", R.GmlTetrahedra,
+                   [(f64, Rd)])
+    kd = I.compile(body("TestFeatures/downlink.cl"), b"downlink", R.GmlTetrahedra,
+                   [(v, Rd | R.GmlRefFlag), (sol, Rd), (res, Wr), (mid, Wr)])
+    ku = I.compile(body("TestFeatures/uplink.cl"), b"uplink", R.GmlVertices,
+                   [(sol, Wr), (mid, Rd | R.GmlVoyeurs)])
+    od = [k for k in R.kernel_objects("downlink") if k >= first][0]
+    ou = [k for k in R.kernel_objects("uplink") if k >= first][0]
+    red, exact, mids, sols = [], [], [], []
+    for i in range(1, EX_ITERS + 1):
+        ctypes.memmove(p + 4, np.float32(i).tobytes(), 4)     # GmlPar->res
+        assert I.L.GmlUploadParameters(I.g) == 1
+        I.launch(kf)
+        I.launch(kd)
+        I.launch(ku)
+        red.append(I.reduce(res, R.GmlSum))
+        r32 = f32(R.kernel_buffers(od)["ResVecTab"], (nt,))
+        exact.append(float(np.sum(r32.astype(np.float64))))
+        mids.append(f32(R.kernel_buffers(od)["TetMidTab"], (nt, 4)))
+        sols.append(f32(R.kernel_buffers(ou)["SolAtVerTab"], (nv, 2, 4)))
+    out.update(ft_mid=np.array(mids), ft_sol=np.array(sols), ft_res=f32(
+        R.kernel_buffers(od)["ResVecTab"], (nt,)), ft_red=np.array(red), ft_red_exact=np.array(exact))
+    I.stop()
+
+    # BallQuality on the triangle square
+    crd2, tri2 = square_mesh()
+    I = R.Instance()
+    I.parameters(8, body("BallQuality/parameters.cl"))
+    v = I.mesh(R.GmlVertices, crd2)
+    tr = I.mesh(R.GmlTriangles, tri2)
+    tq = I.solution(R.GmlTriangles, 1, R.GmlFlt, b"tq")
+    vq = I.solution(R.GmlVertices, 1, R.GmlFlt, b"vq")
+    first = R.lib().refhost_nkernels()
+    k1 = I.compile(body("BallQuality/triqal.cl"), b"triqal", R.GmlTriangles, [(v, Rd), (tq, Wr)])
+    k2 = I.compile(body("BallQuality/verqal.cl"), b"verqal", R.GmlVertices,
+                   [(tr, Rd), (tq, Rd), (vq, Wr)])
+    I.launch(k1)
+    I.launch(k2)
+    o1 = [k for k in R.kernel_objects("triqal") if k >= first][0]
+    o2 = [k for k in R.kernel_objects("verqal") if k >= first][0]
+    out.update(sq_crd=crd2, sq_tri=tri2, bq_tq=f32(R.kernel_buffers(o1)["tqTab"], (len(tri2),)),
+               bq_vq=f32(R.kernel_buffers(o2)["vqTab"], (len(crd2),)))
+    I.stop()
+    np.savez_compressed(os.path.join(OUT, "refhost_examples.npz"), **out)
+    print("refhost_examples.npz", {k: getattr(x, "shape", x) for k, x in out.items()},
+          "residuals", red, exact)
+
+
 CASES = {
     "kuhn_n5": lambda: make_case("refhost_kuhn_n5.npz", "kuhn_n5.npz"),
     "reflected_n6": lambda: make_case("refhost_reflected_n6.npz", "reflected_n6.npz"),
     "linsolve": make_linsolve,
     "c1": make_c1,
     "heat": make_heat,
+    "examples": make_examples,
 }
 
 if __name__ == "__main__":

@@ -245,3 +245,66 @@ def test_compile_error_returns_zero(G, offline, capfd):
                          [(v, G.GmlReadMode, 0), (q, G.GmlWriteMode, 0)])
     assert k == 0
     assert "failed" in capfd.readouterr().out
+
+
+def test_example_flow_bodies_compile(G, offline):
+    """The bodies of tests/test_gpu_examples.py (GpuBandwidth, TestFeatures
+    and BallQuality flows) generate and compile offline with the same
+    datatypes, links and flags."""
+    g = offline
+    crd, tet, v, t = mesh(G, g)
+    Rd, Wr = G.GmlReadMode, G.GmlWriteMode
+    T, V = G.GmlTetrahedra, G.GmlVertices
+    pts = G.lib.GmlNewSolutionData(g, V, 1, G.GmlFlt4, b"Pts")
+    cel = G.lib.GmlNewSolutionData(g, T, 1, G.GmlFlt4, b"Cel")
+    ngb = G.lib.GmlSetNeighbours(g, T)
+    sol = G.lib.GmlNewSolutionData(g, V, 2, G.GmlFlt4, b"Sol")
+    mid = G.lib.GmlNewSolutionData(g, T, 1, G.GmlFlt4, b"Mid")
+    rsd = G.lib.GmlNewSolutionData(g, T, 1, G.GmlFlt, b"Rsd")
+    nbs = G.lib.GmlNewSolutionData(g, T, 1, G.GmlFlt4, b"NbSum")
+    wide = G.lib.GmlNewSolutionData(g, T, 1, G.GmlDbl, b"Wide")
+    assert ngb > 0
+    specs = [("ex_vertex_copy.cl", V, [(v, Rd, 0), (pts, Wr, 0)]),
+             ("ex_tet_nodes.cl", T, [(t, Rd, 0), (cel, Wr, 0)]),
+             ("ex_tet_sum.cl", T, [(v, Rd, 0), (cel, Wr, 0)]),
+             ("ex_ball_sum.cl", V, [(pts, Wr, 0), (cel, Rd, 0)]),
+             ("ex_wide.cl", T, [(wide, Rd, 0)]),
+             ("ex_neighbour_sum.cl", T, [(mid, Rd, ngb), (nbs, Wr, 0)]),
+             ("ex_downlink.cl", T, [(v, Rd | G.GmlRefFlag, 0), (sol, Rd, 0), (rsd, Wr, 0),
+                                    (mid, Wr, 0)]),
+             ("ex_uplink.cl", V, [(sol, Wr, 0), (mid, Rd | G.GmlVoyeurs, 0)])]
+    for f, msh, dats in specs:
+        k = G.compile_kernel(g, body(f), f[:-3], msh, dats)
+        assert k > 0, f
+    s = source(G, g, G.compile_kernel(g, body("ex_neighbour_sum.cl"), "nb2", T,
+                                      [(mid, Rd, ngb), (nbs, Wr, 0)]))
+    assert "MidTab" in s and "NbSumTab[ cnt + count.s1 ] = NbSum;" in s
+
+
+def test_triangle_ball_bodies_compile(G):
+    """The BallQuality flow's bodies over a triangle mesh, offline."""
+    g = G.lib.GmlxInitOffline()
+    assert g
+    try:
+        G.lib.GmlNewParameters(g, 8, PARAMS)
+        v = G.lib.GmlNewMeshData(g, G.GmlVertices, 4)
+        tr = G.lib.GmlNewMeshData(g, G.GmlTriangles, 2)
+        c = np.array([[0, 0, 0, 0], [1, 0, 0, 0], [1, 1, 0, 0], [0, 1, 0, 0]], np.float32)
+        a = np.array([[0, 1, 2], [0, 2, 3]], np.int32)
+        IP = ctypes.POINTER(ctypes.c_int)
+        for typ, arr, n in ((G.GmlVertices, c, 4), (G.GmlTriangles, a, 2)):
+            ref = np.zeros(n, np.int32)
+            assert G.lib.GmlSetDataBlock(g, typ, 0, n - 1, ctypes.c_void_p(arr.ctypes.data),
+                                         ctypes.c_void_p(arr.ctypes.data + (n - 1) * arr.strides[0]),
+                                         ref.ctypes.data_as(IP),
+                                         ctypes.cast(ref.ctypes.data + (n - 1) * 4, IP)) == 1
+        tq = G.lib.GmlNewSolutionData(g, G.GmlTriangles, 1, G.GmlFlt, b"TriQ")
+        tqb = G.lib.GmlNewSolutionData(g, G.GmlTriangles, 1, G.GmlFlt, b"tq")
+        vq = G.lib.GmlNewSolutionData(g, G.GmlVertices, 1, G.GmlFlt, b"vq")
+        k1 = G.compile_kernel(g, body("ex_tri_quality.cl"), "triqal", G.GmlTriangles,
+                              [(v, G.GmlReadMode, 0), (tq, G.GmlWriteMode, 0)])
+        k2 = G.compile_kernel(g, body("ball_min.cl"), "verqal", G.GmlVertices,
+                              [(tr, G.GmlReadMode, 0), (tqb, G.GmlReadMode, 0), (vq, G.GmlWriteMode, 0)])
+        assert k1 > 0 and k2 > 0
+    finally:
+        G.lib.GmlStop(g)

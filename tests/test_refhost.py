@@ -238,3 +238,70 @@ def test_linsolve_restatement_matches_reference_host():
         assert np.max(np.abs(x - r[tag + "_x"])) <= tol * max(1.0, np.max(np.abs(x))), tag
         ax = spmv(lin, col, vals, x0, b, np.float64 if dbl else np.float32)
         assert np.max(np.abs(ax - r[tag + "_ax"])) <= tol * max(1.0, np.max(np.abs(ax))), tag
+
+
+def examples_restated(r):
+    """The GpuBandwidth, TestFeatures and BallQuality flows of
+    make_refhost.make_examples restated in numpy (FP32 where the kernels
+    compute in FP32, sums in the kernels' order)."""
+    crd, tet = r["crd"], r["tet"]
+    nv, nt = len(crd), len(tet)
+    f = np.float32
+    c = crd.astype(f)
+    out = {"bw_ver": c.copy(), "bw_tet_nodes": tet.astype(f)}
+    ts = ((c[tet[:, 0]] + c[tet[:, 1]]) + c[tet[:, 2]]) + c[tet[:, 3]]
+    out["bw_tet_sum"] = ts
+    # balls in increasing tet order, as the tables hold them
+    order = np.argsort(tet.ravel(), kind="stable")
+    owner = tet.ravel()[order]
+    tets = order // 4
+    ball = np.zeros((nv, 4), f)
+    for v_, t_ in zip(owner, tets):
+        ball[v_] = ball[v_] + ts[t_]
+    out["bw_ball"] = ball
+    deg = np.bincount(tet.ravel(), minlength=nv).astype(f)
+    sol = np.full((nv, 2, 4), 0.125, f)
+    mids, sols = [], []
+    for i in range(1, int(len(r["ft_mid"])) + 1):
+        left = ((sol[tet[:, 0], 0] + sol[tet[:, 1], 0]) + sol[tet[:, 2], 0]) + sol[tet[:, 3], 0]
+        right = ((sol[tet[:, 0], 1] + sol[tet[:, 1], 1]) + sol[tet[:, 2], 1]) + sol[tet[:, 3], 1]
+        m = ts * (left + right)
+        m = m / np.sqrt(np.sum(m.astype(np.float64) ** 2, axis=1))[:, None].astype(f)
+        acc = np.zeros((nv, 4), f)
+        for v_, t_ in zip(owner, tets):
+            acc[v_] = acc[v_] + m[t_]
+        sol = np.repeat((f(i) * acc / deg[:, None])[:, None, :], 2, axis=1)
+        mids.append(m)
+        sols.append(sol.copy())
+    out["ft_mid"], out["ft_sol"] = np.array(mids), np.array(sols)
+    out["ft_res"] = np.full(nt, f(nt) / f(len(mids)), f)
+    # triangle quality, 3.4641 |ab x ac| / (hmax (ha + hb + hc)) (1 for an
+    # equilateral triangle), and its vertex-ball minimum
+    p = r["sq_crd"].astype(np.float64)[:, :3]
+    a, b, cc = p[r["sq_tri"][:, 0]], p[r["sq_tri"][:, 1]], p[r["sq_tri"][:, 2]]
+    ha, hb, hc = (np.linalg.norm(b - cc, axis=1), np.linalg.norm(cc - a, axis=1),
+                  np.linalg.norm(a - b, axis=1))
+    s = np.linalg.norm(np.cross(b - a, cc - a), axis=1)
+    out["bq_tq"] = 3.46410 * s / (np.maximum(np.maximum(ha, hb), hc) * (ha + hb + hc))
+    vq = np.full(len(p), np.inf)
+    np.minimum.at(vq, r["sq_tri"].ravel(), np.repeat(r["bq_tq"].astype(np.float64), 3))
+    out["bq_vq"] = vq
+    return out
+
+
+def test_example_flows_restatement_matches_reference_host():
+    r = load("refhost_examples.npz")
+    o = examples_restated(r)
+    for k in ("bw_ver", "bw_tet_nodes", "bw_tet_sum"):
+        assert np.array_equal(o[k], r[k]), k
+    assert np.max(np.abs(o["bw_ball"] - r["bw_ball"])) <= 1e-6 * np.max(np.abs(r["bw_ball"]))
+    for k in ("ft_mid", "ft_sol"):
+        assert np.max(np.abs(o[k] - r[k])) <= 2e-6 * max(1.0, np.max(np.abs(r[k]))), k
+    assert np.array_equal(o["ft_res"], r["ft_res"])
+    nt = len(r["tet"])
+    # the exact residual sums; the reference's own first one misses the
+    # work-groups its calibration launch truncated
+    assert np.allclose(r["ft_red_exact"], [nt * nt / i for i in (1, 2, 3)], rtol=1e-7)
+    assert r["ft_red"][0] < r["ft_red_exact"][0]
+    assert np.max(np.abs(o["bq_tq"] - r["bq_tq"])) <= 2e-6
+    assert np.array_equal(o["bq_vq"].astype(np.float32), r["bq_vq"])
