@@ -84,6 +84,8 @@ def parse():
                         "(capacity)")
     p.add_argument("--serial-requests", type=int, default=200,
                    help="serve: requests of the trace replayed on the serial plain path")
+    p.add_argument("--sweep-seconds", type=float, default=5.0,
+                   help="serve: seconds of arrivals per rate of the p99 capacity sweep (0: none)")
     return p.parse_args()
 
 
@@ -474,7 +476,7 @@ def run_gpu(args, dist):
                               and abs(first.MinQal - port["min"]) <= 2e-5
                               and first.NmbInv == port["inverted"])}
 
-    others = other_configs(G, dev) if dist.world == 1 and not args.no_other_configs else None
+    others = other_configs(G, dev, dist) if dist.world == 1 and not args.no_other_configs else None
 
     G.lib.GmlStop(g)
 
@@ -497,7 +499,7 @@ def run_gpu(args, dist):
         print(json.dumps(line), flush=True)
 
 
-def other_configs(G, dev):
+def other_configs(G, dev, dist):
     """Compact results of the plain-quality configuration (32^3-hex Kuhn
     cube, 196,608 tets: one quality pass with statistics, L2 flushed before
     each of 20 launches), of the solver configuration (96^3-hex SPD
@@ -564,6 +566,28 @@ def other_configs(G, dev):
                               "queue": bo["queue"], "loop": bo["loop"],
                               "speedup_vs_loop": bi["speedup_vs_loop"], "tets": bi["tets"],
                               "frac": bi["roofline"]["frac"], "min_quality": bi["min_quality"]}
+    ns = nodesmooth_measure(G, dev, N_HEX, 5, 3, 0, dist)
+    out["nodesmooth_128cube"] = {
+        "metric": "NodeSmoothing flow through the reference API (generated kernels), GB/s",
+        "unit": "GB/s", "value": round(ns["flow_bytes"] / ns["wall"] / 1e9, 1),
+        "ms_per_flow": round(ns["wall"] * 1e3, 3),
+        "kernels": {k: {"mean_launch_us": v["mean_launch_us"], "frac": v["frac"]}
+                    for k, v in ns["kernels"].items()},
+        "mean_quality_after": ns["q1"] / ns["nt"]}
+    sv = serve_measure(G, dev, 200.0, 10.0, 200, 600, 4.0)
+    out["serve_200rps"] = {
+        "metric": "served requests/s (continuous batching), p50/p99 latency", "unit": "req/s",
+        "value": sv["batching"]["throughput_rps"],
+        "arrivals": "Poisson 200 req/s for 10 s, 50/30/20 quality / smoothing / CG, "
+                    "1e4..1e7 tets, reuse 0.5, 150 GB budget",
+        "batching": {k: sv["batching"][k] for k in ("throughput_rps", "p50_ms", "p99_ms")},
+        "serial_prefix": {k: sv["serial_prefix"][k] for k in ("throughput_rps", "p50_ms", "p99_ms")},
+        "capacity_saturated_ratio": sv["capacity_saturated"].get("batching_over_serial"),
+        "capacity_at_p99": {k: sv["capacity_at_p99"][k] for k in sv["capacity_at_p99"]
+                            if k != "batching" and k != "serial"} | {
+            "batching_max_rate": sv["capacity_at_p99"]["batching"]["max_rate_at_p99"],
+            "serial_max_rate": sv["capacity_at_p99"]["serial"]["max_rate_at_p99"]},
+        "same_result_alone_and_in_mix": "%d of %d" % (sv["same"], sv["nser"])}
     ctypes.CDLL(None).fflush(None)
     return out
 
@@ -868,24 +892,13 @@ def kernel_body(name):
         return f.read()
 
 
-def run_nodesmooth(args, dist):
-    """The reference's NodeSmoothing example flow through the reference API on
-    the smoothing mesh (128^3-hex cube, reflected split): the tet quality
-    body and a sum reduction, then 10 x (scatter: 4 optimal apex points per
-    tet; gather: mean of the ball's points facing each vertex through the
-    vertex -> tet ball with voyeurs, 0.2 relaxation; sum of the squared
-    moves), then the quality and its sum again.  Each GmlReduceVector
-    returns its value to the host, as in the example.  The bodies are this
-    repository's restatements of the example's scatter, gather and quality
-    kernels (tests/kernels).
-    value: algorithmic bytes of the flow / wall time of the flow (GB/s);
-    per-kernel device times with CUDA events over back-to-back launches."""
-    import gmlib_gb300 as G
-    n = args.n
-    dsort = 32 if args.degree_sort else 0
+def nodesmooth_measure(G, dev, n, steps, warmup, dsort, dist):
+    """The NodeSmoothing flow on the n^3-hex cube (see run_nodesmooth);
+    returns the wall time of a flow (median of `steps`), the per-kernel
+    device times and the flow's results."""
     crd, tet, ref = G.cube_mesh(n, split=SPLIT, jitter=JITTER, seed=SEED, degree_sort=dsort)
     nv, nt = len(crd), len(tet)
-    g = G.lib.GmlInit(dist.local)
+    g = G.lib.GmlInit(dev)
     if not g:
         raise SystemExit("GmlInit failed")
     G.lib.GmlxSetTiming(g, 0)
@@ -916,14 +929,14 @@ def run_nodesmooth(args, dist):
         G.lib.GmlLaunchKernel(g, kq)
         return q0, r, G.reduce(g, qal, G.GmlSum)
 
-    for _ in range(max(args.warmup, 3)):          # includes the block-size calibration
+    for _ in range(max(warmup, 3)):               # includes the block-size calibration
         G.lib.GmlxSetData(g, v, G.as_ptr(host_crd), host_crd.nbytes)
         flow()
-    clocks = Clocks(dist.local)
+    clocks = Clocks(dev)
     dist.barrier()
     clocks.start()
     walls = []
-    for _ in range(args.steps):
+    for _ in range(steps):
         G.lib.GmlxSetData(g, v, G.as_ptr(host_crd), host_crd.nbytes)
         G.lib.GmlxSynchronize(g)
         ts = time.perf_counter()
@@ -957,31 +970,55 @@ def run_nodesmooth(args, dist):
     kern = {k: {"mean_launch_us": round(per[k] * 1e6, 2), "block": blk[k], "registers": regs[k],
                 "algorithmic_bytes": kb[k], "achieved": round(kb[k] / per[k] / 1e9, 1),
                 "frac": round(kb[k] / per[k] / 1e9 / peak, 4)} for k in per}
+    return {"nv": nv, "nt": nt, "tet": tet, "wall": wall, "flow_bytes": flow_bytes,
+            "kernels": kern, "peak": peak, "peak_src": peak_src, "clocks": clk,
+            "q0": q0, "q1": q1, "r": r, "kb": kb}
+
+
+def run_nodesmooth(args, dist):
+    """The reference's NodeSmoothing example flow through the reference API on
+    the smoothing mesh (128^3-hex cube, reflected split): the tet quality
+    body and a sum reduction, then 10 x (scatter: 4 optimal apex points per
+    tet; gather: mean of the ball's points facing each vertex through the
+    vertex -> tet ball with voyeurs, 0.2 relaxation; sum of the squared
+    moves), then the quality and its sum again.  Each GmlReduceVector
+    returns its value to the host, as in the example.  The bodies are this
+    repository's restatements of the example's scatter, gather and quality
+    kernels (tests/kernels).
+    value: algorithmic bytes of the flow / wall time of the flow (GB/s);
+    per-kernel device times with CUDA events over back-to-back launches."""
+    import gmlib_gb300 as G
+    n = args.n
+    dsort = 32 if args.degree_sort else 0
+    m = nodesmooth_measure(G, dist.local, n, args.steps, args.warmup, dsort, dist)
+    nv, nt, kern = m["nv"], m["nt"], m["kernels"]
     if dist.rank == 0:
         line = {"metric": "NodeSmoothing flow through the reference API, GB/s",
-                "value": round(dist.world * flow_bytes / wall / 1e9, 1), "unit": "GB/s",
+                "value": round(dist.world * m["flow_bytes"] / m["wall"] / 1e9, 1), "unit": "GB/s",
                 "n_gpus": dist.world, "steps": args.steps, "warmup": max(args.warmup, 3),
-                "ms_per_step": round(wall * 1e3, 3), "higher_is_better": True,
+                "ms_per_step": round(m["wall"] * 1e3, 3), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": "NodeSmoothing example flow (quality + sum, 10 x "
                                        "(scatter, gather, residual sum), quality + sum), "
                                        "%d^3-hex cube, reflected split" % n,
                            "numbering": "Hilbert, then vertices in at most 32 tets first "
                                         "(GmlxDegreeSort)" if dsort else "Hilbert",
-                           "tets": nt, "vertices": nv, "vertex_tet_degrees": degree_summary([tet]),
+                           "tets": nt, "vertices": nv,
+                           "vertex_tet_degrees": degree_summary([m["tet"]]),
                            "l2": "inputs larger than L2 (OptCrd alone is %.0f MB)" % (64e-6 * nt),
                            "step": "wall clock of the flow, host reductions included; the "
                                    "coordinates are re-uploaded before each step, outside it"},
                 "gpu_launches": args.steps * (22 + 12),
                 "roofline": {"bound": "hbm", "kernel": "gather (generated)",
-                             "achieved": kern["gather"]["achieved"], "peak": peak, "unit": "GB/s",
-                             "frac": kern["gather"]["frac"], "traffic": None,
-                             "algorithmic_bytes_per_launch": kb["gather"],
+                             "achieved": kern["gather"]["achieved"], "peak": m["peak"],
+                             "unit": "GB/s", "frac": kern["gather"]["frac"], "traffic": None,
+                             "algorithmic_bytes_per_launch": m["kb"]["gather"],
                              "mean_launch_us": kern["gather"]["mean_launch_us"],
-                             "peak_source": peak_src},
-                "kernels": kern, "clocks": clk,
-                "result_check": {"mean_quality_before": q0 / nt, "mean_quality_after": q1 / nt,
-                                 "last_residual": r}}
+                             "peak_source": m["peak_src"]},
+                "kernels": kern, "clocks": m["clocks"],
+                "result_check": {"mean_quality_before": m["q0"] / nt,
+                                 "mean_quality_after": m["q1"] / nt,
+                                 "last_residual": m["r"]}}
         print(json.dumps(line), flush=True)
 
 
@@ -1193,76 +1230,133 @@ def run_batch(args, dist):
 SERVE_BUCKETS = 12
 
 
-def run_serve(args, dist):
-    """Poisson arrivals (--rate per s for --duration s), 50/30/20 quality /
-    10-sweep smoothing / CG requests on meshes of 1e4..1e7 tets (log-uniform)
-    and on the SPD systems of their vertex graphs; a request targets a mesh
-    seen before with probability 0.5, else a new one.  Distinct sizes come
-    from a pool of size buckets (each new target is a separate resident
-    copy).  Continuous batching with a 150 GB budget, then the serial plain
-    path on the first --serial-requests requests of the same trace."""
-    import gmlib_gb300 as G
-    rng = np.random.default_rng(SEED)
-    ns = np.unique(np.round(np.exp(np.linspace(np.log((1e4 / 6) ** (1 / 3)),
-                                               np.log((1e7 / 6) ** (1 / 3)),
-                                               SERVE_BUCKETS))).astype(int))
-    t0 = time.time()
-    meshes = gen_meshes([(int(n), 1, 0.3, SEED + i) for i, n in enumerate(ns)])
-    systems = [G.cube_spd(int(n), 0, seed=SEED + i) for i, n in enumerate(ns)]
-    tgen = time.time() - t0
-    logt = np.log(6.0 * ns.astype(np.float64) ** 3)
+SERVE_P99_MS = 100.0                       # the stated p99 of the capacity sweep
+SERVE_SWEEP_RATES = (100, 150, 200, 300, 400, 500, 600, 800)
 
-    def bucket(x):
-        return int(np.argmin(np.abs(logt - x)))
-    def register(server, cls, b):
+
+class ServePool:
+    """Config-5 targets: meshes of 1e4..1e7 tets (log-uniform buckets, config-2
+    construction) and the SPD block systems of their vertex graphs (config-3
+    construction), generated in parallel (the library calls release the GIL)."""
+
+    def __init__(self, G):
+        from concurrent.futures import ThreadPoolExecutor
+        self.G = G
+        self.ns = np.unique(np.round(np.exp(np.linspace(np.log((1e4 / 6) ** (1 / 3)),
+                                                        np.log((1e7 / 6) ** (1 / 3)),
+                                                        SERVE_BUCKETS))).astype(int))
+        t0 = time.time()
+        self.meshes = gen_meshes([(int(n), 1, 0.3, SEED + i) for i, n in enumerate(self.ns)])
+        with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+            self.systems = list(ex.map(lambda a: G.cube_spd(int(a[1]), 0, seed=SEED + a[0]),
+                                       enumerate(self.ns)))
+        self.tgen = time.time() - t0
+        self.logt = np.log(6.0 * self.ns.astype(np.float64) ** 3)
+
+    def bucket(self, x):
+        return int(np.argmin(np.abs(self.logt - x)))
+
+    def register(self, server, cls, b):
+        G = self.G
         if cls == 0:
-            crd, tet, ref = meshes[b]
+            crd, tet, ref = self.meshes[b]
             return G.lib.GmlxServeAddMesh(server, len(crd), G.as_ptr(crd), G.as_ptr(ref),
-                                          len(tet), G.as_ptr(tet), 1.0 / ns[b])
-        lin, col, val, rhs = systems[b]
+                                          len(tet), G.as_ptr(tet), 1.0 / self.ns[b])
+        lin, col, val, rhs = self.systems[b]
         return G.lib.GmlxServeAddSystem(server, len(lin) - 1, len(col), G.as_ptr(lin),
                                         G.as_ptr(col), G.as_ptr(val), G.as_ptr(rhs))
 
-    srv = G.lib.GmlxServeNew(dist.local, 150e9, 8)
+
+def serve_trace(G, pool, srv, nreq, rate, rng):
+    """Poisson arrivals at `rate`; 50/30/20 quality / smoothing / CG; a request
+    targets a known target with probability 0.5, else registers a new one.
+    Returns (requests, [(class, bucket)] registered in order)."""
     added = []
-    nreq = int(args.rate * args.duration)
-    req = (G.GmlxRequest * nreq)()
+    req = (G.GmlxRequest * max(nreq, 1))()
     seen = {0: [], 1: []}
     t = 0.0
-    kinds = []
     for i in range(nreq):
-        t += rng.exponential(1.0 / args.rate)
+        t += rng.exponential(1.0 / rate)
         u = rng.random()
         kind = G.GmlxReqQuality if u < 0.5 else (G.GmlxReqSmooth if u < 0.8 else G.GmlxReqSolve)
         cls = 1 if kind == G.GmlxReqSolve else 0
         if seen[cls] and rng.random() < 0.5:
             target = int(rng.choice(seen[cls]))
         else:
-            b = bucket(rng.uniform(np.log(1e4), np.log(1e7)))
-            target = register(srv, cls, b)
+            b = pool.bucket(rng.uniform(np.log(1e4), np.log(1e7)))
+            target = pool.register(srv, cls, b)
             added.append((cls, b))
             seen[cls].append(target)
         req[i].kind, req[i].target, req[i].arrival = kind, target, t
-        kinds.append(kind)
+    return req, added
+
+
+def serve_stats(st):
+    return {"completed": st.completed, "failed": st.failed, "seconds": round(st.seconds, 2),
+            "throughput_rps": round(st.throughput, 2), "p50_ms": round(st.p50 * 1e3, 2),
+            "p99_ms": round(st.p99 * 1e3, 2), "max_ms": round(st.max * 1e3, 2),
+            "loads": st.loads, "evictions": st.evictions,
+            "peak_resident_gb": round(st.peak_bytes / 1e9, 2)}
+
+
+def serve_p99_sweep(G, pool, dev, duration, rates, p99_ms):
+    """Highest arrival rate each path sustains with its p99 latency at or
+    below p99_ms: for each rate in increasing order, a fresh server (same
+    pool, nothing resident) replays `duration` s of the config-5 trace at
+    that rate; a path stops at the first rate whose p99 exceeds the target
+    or that leaves requests unfinished."""
+    out = {}
+    for mode, name in ((G.GmlxServeBatching, "batching"), (G.GmlxServeSerial, "serial")):
+        runs, best = [], 0.0
+        for rate in rates:
+            srv = G.lib.GmlxServeNew(dev, 150e9, 8)
+            req, _ = serve_trace(G, pool, srv, int(rate * duration), rate,
+                                 np.random.default_rng(SEED))
+            st = G.GmlxServeStats()
+            G.lib.GmlxServeRun(srv, req, int(rate * duration), mode, ctypes.byref(st))
+            G.lib.GmlxServeFree(srv)
+            ok = st.failed == 0 and st.completed == int(rate * duration) and st.p99 * 1e3 <= p99_ms
+            runs.append({"rate": rate, "p50_ms": round(st.p50 * 1e3, 2),
+                         "p99_ms": round(st.p99 * 1e3, 2), "throughput_rps": round(st.throughput, 2),
+                         "meets_p99": bool(ok)})
+            if not ok:
+                break
+            best = float(rate)
+        out[name] = {"max_rate_at_p99": best, "runs": runs}
+    if out["serial"]["max_rate_at_p99"] > 0:
+        out["batching_over_serial"] = round(out["batching"]["max_rate_at_p99"]
+                                            / out["serial"]["max_rate_at_p99"], 2)
+    out["p99_target_ms"] = p99_ms
+    out["seconds_per_run"] = duration
+    return out
+
+
+def serve_measure(G, dev, rate, duration, serial_requests, saturate, sweep_s, pool=None):
+    """Config 5 (see run_serve); returns the measured dict."""
+    pool = pool or ServePool(G)
+    rng = np.random.default_rng(SEED)
+    srv = G.lib.GmlxServeNew(dev, 150e9, 8)
+    nreq = int(rate * duration)
+    req, added = serve_trace(G, pool, srv, nreq, rate, rng)
     stb = G.GmlxServeStats()
-    clocks = Clocks(dist.local)
+    clocks = Clocks(dev)
     clocks.start()
     G.lib.GmlxServeRun(srv, req, nreq, G.GmlxServeBatching, ctypes.byref(stb))
     clk = clocks.stop()
-    nser = min(nreq, args.serial_requests)
+    nser = min(nreq, serial_requests)
     ser = (G.GmlxRequest * max(nser, 1))()
     for i in range(nser):
         ser[i].kind, ser[i].target, ser[i].arrival = req[i].kind, req[i].target, req[i].arrival
     sts = G.GmlxServeStats()
     G.lib.GmlxServeRun(srv, ser, nser, G.GmlxServeSerial, ctypes.byref(sts))
-    # capacity: the first --saturate requests of the trace all due at t = 0,
+    # capacity: the first `saturate` requests of the trace all due at t = 0,
     # through each path (requests/s the path sustains when never idle), on a
     # second server with the same targets and none of them resident
-    nsat = min(nreq, args.saturate)
+    nsat = min(nreq, saturate)
     cap = {}
-    srv2 = G.lib.GmlxServeNew(dist.local, 150e9, 8)
+    srv2 = G.lib.GmlxServeNew(dev, 150e9, 8)
     for cls, b in added:
-        register(srv2, cls, b)
+        pool.register(srv2, cls, b)
     for mode, name in ((G.GmlxServeBatching, "batching"), (G.GmlxServeSerial, "serial")):
         sat = (G.GmlxRequest * max(nsat, 1))()
         for i in range(nsat):
@@ -1275,6 +1369,7 @@ def run_serve(args, dist):
     if cap["serial"]["throughput_rps"] > 0:
         cap["batching_over_serial"] = round(cap["batching"]["throughput_rps"]
                                             / cap["serial"]["throughput_rps"], 2)
+
     def breakdown(reqs, n):
         """per kind: mean queueing delay (start - arrival) and service time
         (finish - start), split by whether the request loaded its target"""
@@ -1305,25 +1400,41 @@ def run_serve(args, dist):
                and (req[i].NmbIte, req[i].RelRes, req[i].qal.MinQal, req[i].qal.MinIdx)
                == (ser[i].NmbIte, ser[i].RelRes, ser[i].qal.MinQal, ser[i].qal.MinIdx))
     G.lib.GmlxServeFree(srv)
+    sweep = serve_p99_sweep(G, pool, dev, sweep_s, SERVE_SWEEP_RATES, SERVE_P99_MS) \
+        if sweep_s > 0 else None
+    return {"pool": pool, "batching": serve_stats(stb), "batching_by_kind": bd,
+            "serial_prefix": serve_stats(sts), "capacity_saturated": cap,
+            "capacity_at_p99": sweep, "same": same, "nser": nser, "clocks": clk}
 
-    def d(st):
-        return {"completed": st.completed, "failed": st.failed, "seconds": round(st.seconds, 2),
-                "throughput_rps": round(st.throughput, 2), "p50_ms": round(st.p50 * 1e3, 2),
-                "p99_ms": round(st.p99 * 1e3, 2), "max_ms": round(st.max * 1e3, 2),
-                "loads": st.loads, "evictions": st.evictions,
-                "peak_resident_gb": round(st.peak_bytes / 1e9, 2)}
+
+def run_serve(args, dist):
+    """Poisson arrivals (--rate per s for --duration s), 50/30/20 quality /
+    10-sweep smoothing / CG requests on meshes of 1e4..1e7 tets (log-uniform)
+    and on the SPD systems of their vertex graphs; a request targets a mesh
+    seen before with probability 0.5, else a new one.  Distinct sizes come
+    from a pool of size buckets (each new target is a separate resident
+    copy).  Continuous batching with a 150 GB budget, then the serial plain
+    path on the first --serial-requests requests of the same trace, the
+    saturated capacity of both paths, and the highest rate each path
+    sustains at the stated p99 (--sweep-seconds of arrivals per rate)."""
+    import gmlib_gb300 as G
+    m = serve_measure(G, dist.local, args.rate, args.duration, args.serial_requests,
+                      args.saturate, args.sweep_seconds)
+    pool = m["pool"]
     if dist.rank == 0:
         line = {"metric": "served requests/s at p99 (continuous batching)",
-                "value": round(stb.throughput, 2), "unit": "req/s", "n_gpus": dist.world,
+                "value": m["batching"]["throughput_rps"], "unit": "req/s", "n_gpus": dist.world,
                 "higher_is_better": True, "dtype": "f32 / f64", "data": "synthetic",
                 "config": {"workload": "Poisson %.0f req/s for %.0f s, 50/30/20 quality / "
                                        "10-sweep smoothing / CG (1e-10)" % (args.rate, args.duration),
-                           "sizes_tets": [int(6 * n ** 3) for n in ns], "reuse": 0.5,
-                           "budget_gb": 150, "slots": 8, "pool_generation_s": round(tgen, 1),
-                           "vertex_tet_degrees": degree_summary([m[1] for m in meshes])},
-                "batching": d(stb), "batching_by_kind": bd, "serial_prefix": d(sts),
-                "capacity_saturated": cap,
-                "same_result_alone_and_in_mix": "%d of %d" % (same, nser), "clocks": clk}
+                           "sizes_tets": [int(6 * n ** 3) for n in pool.ns], "reuse": 0.5,
+                           "budget_gb": 150, "slots": 8, "pool_generation_s": round(pool.tgen, 1),
+                           "vertex_tet_degrees": degree_summary([x[1] for x in pool.meshes])},
+                "batching": m["batching"], "batching_by_kind": m["batching_by_kind"],
+                "serial_prefix": m["serial_prefix"], "capacity_saturated": m["capacity_saturated"],
+                "capacity_at_p99": m["capacity_at_p99"],
+                "same_result_alone_and_in_mix": "%d of %d" % (m["same"], m["nser"]),
+                "clocks": m["clocks"]}
         print(json.dumps(line), flush=True)
 
 

@@ -4,7 +4,7 @@
  * workloads directly instead of through generated scatter/gather pairs).
  *
  * Topology (built on the GPU, deterministic):
- *   vertex -> tetrahedron CSR   count (atomics), single-block exclusive scan,
+ *   vertex -> tetrahedron CSR   count (atomics), exclusive scan (gml_scan.cu),
  *                               fill (atomic slots; order within a ball is
  *                               not used by the kernels below)
  *   ball of points              per vertex, the distinct vertices of its
@@ -15,11 +15,13 @@
  *   boundary vertices           vertices of faces owned by a single tet
  *
  * Hot kernels (HBM-bound):
- *   laplace_sell   one Jacobi sweep x' = x + w (mean(ball) - x), one thread
+ *   laplace_pf_kernel
+ *                  one Jacobi sweep x' = x + w (mean(ball) - x), one thread
  *                  per row; per vertex 4 (packed row word) + 4 deg (entries,
  *                  128-byte runs per warp) + 16 (own) + 16 (write) bytes;
  *                  neighbour gathers hit L2 (the coordinates are 16 V bytes).
- *   tet_quality    mean-ratio quality 12 (3|V|)^(2/3) / sum l^2 signed by
+ *   tet_quality_tma_kernel
+ *                  mean-ratio quality 12 (3|V|)^(2/3) / sum l^2 signed by
  *                  orientation, 64-bin histogram, min/argmin, max/argmax,
  *                  sum, inverted-element count and bit flags; the 16 bytes
  *                  per tet of connectivity are staged through shared memory
