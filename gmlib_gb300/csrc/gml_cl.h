@@ -501,6 +501,61 @@ template<class T> GML_FN T gml_ld_cs(const T *p)
    return *p;
 }
 
+/* Write a line of NI 16-byte items (NI = 2 or 4) with 32-byte stores
+   (st.global.v8.b32): one full sector per store, where 16-byte stores from
+   the lanes of a warp, a line apart, each wrote half sectors.  The values
+   written are the items' bytes unchanged.  Lines that are not 32-byte
+   aligned are written item by item. */
+template<class T, int NI> GML_FN void gml_store_line(T (&dst)[NI], const T (&v)[NI])
+{
+   static_assert(sizeof(T) == 16 && (NI == 2 || NI == 4), "16-byte items, 2 or 4 per line");
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+   if((((unsigned long long)(&dst[0])) & 31) == 0)
+   {
+#pragma unroll
+      for(int h=0;h<NI;h+=2)
+      {
+         uint4 a, b;
+         memcpy(&a, &v[h], 16);
+         memcpy(&b, &v[h + 1], 16);
+         asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+                      :: "l"(&dst[h]), "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w),
+                         "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w) : "memory");
+      }
+      return;
+   }
+#endif
+#pragma unroll
+   for(int j=0;j<NI;j++)
+      dst[j] = v[j];
+}
+
+/* Read a line of NI 16-byte items (NI = 2 or 4) with 32-byte loads
+   (ld.global.v8.b32), the counterpart of gml_store_line. */
+template<class T, int NI> GML_FN void gml_load_line(T (&v)[NI], const T (&src)[NI])
+{
+   static_assert(sizeof(T) == 16 && (NI == 2 || NI == 4), "16-byte items, 2 or 4 per line");
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+   if((((unsigned long long)(&src[0])) & 31) == 0)
+   {
+#pragma unroll
+      for(int h=0;h<NI;h+=2)
+      {
+         uint4 a, b;
+         asm volatile("ld.global.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                      : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w),
+                        "=r"(b.x), "=r"(b.y), "=r"(b.z), "=r"(b.w) : "l"(&src[h]));
+         memcpy(&v[h], &a, 16);
+         memcpy(&v[h + 1], &b, 16);
+      }
+      return;
+   }
+#endif
+#pragma unroll
+   for(int j=0;j<NI;j++)
+      v[j] = src[j];
+}
+
 template<class T, int NI> struct gml_up_row
 {
    const T *p;

@@ -302,8 +302,13 @@ int gml_generate(char **res, const char *PrcNam, int MshTyp, int NmbArg,
       if(lazy && a->LnkDir == 1 && a->NmbItm > 1)
          continue;
 
-      for(j=0;j<a->NmbItm;j++)
-         emit_eager_item(&o, a, lnk, cpt, j);
+      if(lazy && !lnk && !cpt && a->LnkDir != 1 && !(a->FlgTab & GmlVoyeurs)
+      && GmlOclTypSiz[ a->ItmTyp ] == 16 && (a->NmbItm == 2 || a->NmbItm == 4))
+         /* the entity's own 32- or 64-byte line: 32-byte loads */
+         emit(&o, "   gml_load_line(%s, %sTab[ cnt + count.s1 ]);\n", a->nam, a->nam);
+      else
+         for(j=0;j<a->NmbItm;j++)
+            emit_eager_item(&o, a, lnk, cpt, j);
       emit(&o, "\n");
    }
 
@@ -365,6 +370,9 @@ int gml_generate(char **res, const char *PrcNam, int MshTyp, int NmbArg,
 
       if(a->NmbItm == 1)
          emit(&o, "   %sTab[ cnt + count.s1 ] = %s;\n", a->nam, a->nam);
+      else if(GmlOclTypSiz[ a->ItmTyp ] == 16 && (a->NmbItm == 2 || a->NmbItm == 4))
+         /* a 32- or 64-byte line of 16-byte items: 32-byte stores */
+         emit(&o, "   gml_store_line(%sTab[ cnt + count.s1 ], %s);\n", a->nam, a->nam);
       else
          for(j=0;j<a->NmbItm;j++)
             emit(&o, "   %sTab[ cnt + count.s1 ][%d] = %s[%d];\n", a->nam, j, a->nam, j);

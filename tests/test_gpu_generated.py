@@ -347,3 +347,65 @@ def test_calibration_is_kept_in_the_tuning_file(tmp_path):
                            text=True, timeout=300)
     assert again.returncode == 0, again.stderr
     assert int(again.stdout.split()[-1]) == chosen
+
+
+def _line_items_expected(a, b, c, d):
+    ea = np.stack([a[:, 1] + a[:, 2], a[:, 2] - a[:, 0], a[:, 3] + a[:, 3], a[:, 0] - a[:, 1]], 1)
+    ec = np.stack([c[:, 3], c[:, 2] + c[:, 0], c[:, 1] - c[:, 3], c[:, 0]], 1)
+    eb = np.stack([b[:, 1], b[:, 0] + b[:, 0]], 1)
+    ed = np.stack([d[:, 1] + d[:, 0], d[:, 0] - d[:, 1]], 1)
+    return ea, eb, ec, ed
+
+
+def test_line_items_load_and_store(G, gpu):
+    """Lines of 2 and 4 sixteen-byte items (float4, int4, double2), read and
+    written whole by a tet kernel (32-byte loads and stores), against numpy;
+    plus a vertex kernel rewriting its own 4-item line with a ball sum, whose
+    high-degree twin launch starts at a line offset."""
+    crd, tet, ref = G.cube_mesh(12, split=1, jitter=0.2, seed=5)
+    nv, nt = len(crd), len(tet)
+    v, t = setup_mesh(G, gpu, crd, tet, ref)
+    rng = np.random.default_rng(11)
+    a = rng.standard_normal((nt, 4, 4)).astype(np.float32)
+    b = rng.standard_normal((nt, 2, 4)).astype(np.float32)
+    c = rng.integers(-1000, 1000, (nt, 4, 4)).astype(np.int32)
+    d = rng.standard_normal((nt, 2, 2))
+    ia = G.lib.GmlNewSolutionData(gpu, G.GmlTetrahedra, 4, G.GmlFlt4, b"A")
+    ib = G.lib.GmlNewSolutionData(gpu, G.GmlTetrahedra, 2, G.GmlFlt4, b"B")
+    ic = G.lib.GmlNewSolutionData(gpu, G.GmlTetrahedra, 4, G.GmlInt4, b"C")
+    idd = G.lib.GmlNewSolutionData(gpu, G.GmlTetrahedra, 2, G.GmlDbl2, b"D")
+    for idx, x in ((ia, a), (ib, b), (ic, c), (idd, d)):
+        assert G.set_data(gpu, idx, x) == 1
+    RW = G.GmlReadMode | G.GmlWriteMode
+    k = G.compile_kernel(gpu, body("line_items.cl"), "line_items", G.GmlTetrahedra,
+                         [(ia, RW, 0), (ib, RW, 0), (ic, RW, 0), (idd, RW, 0)])
+    assert k and G.lib.GmlxKernelIsLazy(gpu, k) == 1
+    src = G.lib.GmlxKernelSource(gpu, k)
+    src = ctypes.string_at(src).decode() if isinstance(src, int) else src.decode()
+    assert "gml_load_line(A, ATab[ cnt + count.s1 ]);" in src
+    assert "gml_store_line(DTab[ cnt + count.s1 ], D);" in src
+    assert G.lib.GmlLaunchKernel(gpu, k) == 1
+    ea, eb, ec, ed = _line_items_expected(a, b, c, d)
+    assert np.array_equal(G.get_data(gpu, ia, np.float32, (nt, 4, 4)), ea)
+    assert np.array_equal(G.get_data(gpu, ib, np.float32, (nt, 2, 4)), eb)
+    assert np.array_equal(G.get_data(gpu, ic, np.int32, (nt, 4, 4)), ec)
+    assert np.array_equal(G.get_data(gpu, idd, np.float64, (nt, 2, 2)), ed)
+
+    # vertex lines, through the base and the high ball tables
+    q = rng.standard_normal(nt).astype(np.float32)
+    v4 = rng.standard_normal((nv, 4, 4)).astype(np.float32)
+    iq = G.lib.GmlNewSolutionData(gpu, G.GmlTetrahedra, 1, G.GmlFlt, b"Q")
+    iv = G.lib.GmlNewSolutionData(gpu, G.GmlVertices, 4, G.GmlFlt4, b"V4")
+    assert G.set_data(gpu, iq, q) == 1 and G.set_data(gpu, iv, v4) == 1
+    kb = G.compile_kernel(gpu, body("line_items_ball.cl"), "line_items_ball", G.GmlVertices,
+                          [(iv, RW, 0), (iq, G.GmlReadMode, 0)])
+    assert kb
+    assert G.lib.GmlLaunchKernel(gpu, kb) == 1
+    got = G.get_data(gpu, iv, np.float32, (nv, 4, 4))
+    s = np.zeros(nv, np.float64)
+    np.add.at(s, tet.reshape(-1), np.repeat(q.astype(np.float64), 4))
+    want = np.stack([v4[:, 3] + s[:, None], v4[:, 0] + v4[:, 1], v4[:, 1] - v4[:, 2],
+                     v4[:, 2] + v4[:, 0]], 1)
+    # items 1..3 are exact; item 0 holds an FP32 ball sum (order differs)
+    assert np.array_equal(got[:, 1:], want[:, 1:].astype(np.float32))
+    assert np.max(np.abs(got[:, 0] - want[:, 0])) <= 1e-5 * max(1.0, float(np.abs(want[:, 0]).max()))
