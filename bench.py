@@ -574,7 +574,7 @@ def other_configs(G, dev, dist):
         "kernels": {k: {"mean_launch_us": v["mean_launch_us"], "frac": v["frac"]}
                     for k, v in ns["kernels"].items()},
         "mean_quality_after": ns["q1"] / ns["nt"]}
-    sv = serve_measure(G, dev, 200.0, 10.0, 200, 600, 4.0)
+    sv = serve_in_fresh_process(dev)
     out["serve_200rps"] = {
         "metric": "served requests/s (continuous batching), p50/p99 latency", "unit": "req/s",
         "value": sv["batching"]["throughput_rps"],
@@ -1231,7 +1231,27 @@ SERVE_BUCKETS = 12
 
 
 SERVE_P99_MS = 100.0                       # the stated p99 of the capacity sweep
-SERVE_SWEEP_RATES = (100, 150, 200, 300, 400, 500, 600, 800)
+SERVE_SWEEP_RATES = (50, 100, 150, 200, 300, 400, 600)
+
+
+def serve_in_fresh_process(dev):
+    """Config 5 for the default line (10 s at 200 req/s, 4-s sweep runs),
+    measured by `bench.py --workload serve` in a process of its own: serve
+    runs that follow other heavy workloads in one process measure slower
+    (host-side state), so the default line does not inherit the others'."""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--workload", "serve",
+           "--duration", "10", "--sweep-seconds", "4"]
+    env = dict(os.environ, LOCAL_RANK=str(dev), RANK="0", WORLD_SIZE="1")
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, env=env)
+    for line in r.stdout.splitlines():
+        if line.startswith("{"):
+            d = json.loads(line)
+            c = d["capacity_at_p99"]
+            return {"batching": d["batching"], "serial_prefix": d["serial_prefix"],
+                    "capacity_saturated": d["capacity_saturated"], "capacity_at_p99": c,
+                    "same": int(d["same_result_alone_and_in_mix"].split()[0]),
+                    "nser": int(d["same_result_alone_and_in_mix"].split()[-1])}
+    raise SystemExit("the serve run failed:\n" + r.stdout[-2000:] + r.stderr[-2000:])
 
 
 class ServePool:

@@ -437,12 +437,28 @@ static int direct_ok(GmlSct *gml, GmlDatSct *dat, const void *buf, size_t bytes)
        && gmd_host_addressable(gml->dev, buf);
 }
 
+/* A datatype's mirror is rewritten whole: a refresh still owed to it is
+   dropped (it would be overwritten), the ones owed to other datatypes wait
+   (their device data do not change here). */
+static void drop_refresh(GmlSct *gml, GmlDatSct *dat)
+{
+   if(dat->MirOld)
+   {
+      dat->MirOld = 0;
+      gml->NmbMirOld--;
+   }
+}
+
 int GmlxSetData(size_t GmlIdx, int DatIdx, const void *buf, size_t bytes)
 {
-   GETGMLPTR(gml, GmlIdx);
+   GETGMLPTR_NOSETTLE(gml, GmlIdx);
    GmlDatSct *dat = get_dat(gml, DatIdx);
    if(!dat || !dat->CpuMem || bytes != dat->MemSiz)
+   {
+      gml_settle(gml);
       return 0;
+   }
+   drop_refresh(gml, dat);
    gml_wait_upload(gml, dat);
    /* direct only when idle: the copy must land before the call returns (the
       caller may reuse buf), and waiting behind queued kernels would make an
@@ -461,23 +477,35 @@ int GmlxSetData(size_t GmlIdx, int DatIdx, const void *buf, size_t bytes)
 
 int GmlxGetData(size_t GmlIdx, int DatIdx, void *buf, size_t bytes)
 {
-   GETGMLPTR(gml, GmlIdx);
+   GETGMLPTR_NOSETTLE(gml, GmlIdx);
    GmlDatSct *dat = get_dat(gml, DatIdx);
    if(!dat || !dat->CpuMem || bytes != dat->MemSiz)
+   {
+      gml_settle(gml);
       return 0;
+   }
    if(direct_ok(gml, dat, buf, bytes))
    {
       /* ordered after the kernels that produced the data; the mirror is
-         refreshed as a download would */
+         refreshed at the next call on the instance (gml_settle), where a
+         download would have refreshed it here: until then nothing can
+         read it or change the device data.  Reads of other datatypes whose
+         refresh is owed leave theirs owed too. */
       gml_wait_upload(gml, dat);
-      if(gmd_fanout(gml->dev, dat->GpuMem, buf, dat->CpuMem, bytes))
+      if(gmd_fanout(gml->dev, dat->GpuMem, buf, NULL, bytes))
       {
          if(!gmd_sync(gml->dev))
             return 0;
+         if(!dat->MirOld)
+         {
+            dat->MirOld = 1;
+            gml->NmbMirOld++;
+         }
          gml->MovSiz += bytes;
          return 1;
       }
    }
+   drop_refresh(gml, dat);
    if(!gml_download(gml, DatIdx) && bytes)
       return 0;
    gml_host_copy(buf, dat->CpuMem, bytes);

@@ -37,6 +37,7 @@ typedef struct
    void        *GpuMem, *CpuMem;
    int         pinned;
    void        *UpEvt;        /* event recorded after the last async upload */
+   int         MirOld;        /* mirror still to be refreshed from the device (GmlxGetData) */
 }GmlDatSct;
 
 /* One generated-kernel argument; fields and meanings follow ArgSct of the
@@ -116,11 +117,20 @@ typedef struct
    int         PinOff;                /* 1: pageable host mirrors (no page locking) */
    char        **Names;               /* interned strings owned by the instance */
    int         NmbNames, CapNames;
+   int         NmbMirOld;             /* datatypes whose MirOld is set */
    void        *ext;                  /* state of the native extensions */
    void        *bat;                  /* batched meshes (gml_batch.c) */
 }GmlSct;
 
-#define GETGMLPTR(p,i)  GmlSct *p = (GmlSct *)(i)
+/* Every entry point starts here.  A bulk read (GmlxGetData) leaves the host
+   mirror of its datatype to be refreshed; the next call on the instance
+   refreshes it before anything can read the mirror or change the device
+   data (gml_settle), so the mirror holds the data of the read, as after a
+   download.  GmlxSetData and GmlxGetData, which rewrite or keep that data,
+   use GETGMLPTR_NOSETTLE. */
+#define GETGMLPTR_NOSETTLE(p,i)  GmlSct *p = (GmlSct *)(i)
+#define GETGMLPTR(p,i)  GmlSct *p = (GmlSct *)(i); gml_settle(p)
+void  gml_settle(GmlSct *gml);
 
 /* shared tables (gml_tables.c) */
 extern const int   GmlOclTypSiz[ GmlMaxOclTyp ];

@@ -171,6 +171,24 @@ int gml_download(GmlSct *gml, int idx)
    return (int)(dat->MemSiz > 0x7fffffff ? 0x7fffffff : dat->MemSiz);
 }
 
+/* Refresh the host mirrors that bulk reads left to the next call (see
+   GETGMLPTR): one blocking download each, of device data that nothing has
+   changed since the read. */
+void gml_settle(GmlSct *gml)
+{
+   int i;
+
+   if(!gml || !gml->NmbMirOld)
+      return;
+   for(i=1;i<=GmlMaxDat;i++)
+      if(gml->dat[i].use && gml->dat[i].MirOld)
+      {
+         gml->dat[i].MirOld = 0;
+         gml_download(gml, i);
+      }
+   gml->NmbMirOld = 0;
+}
+
 /* Spread an arbitrary vector size over power-of-two OpenCL vectors of at most
    16 lanes (reference GetCntVec, :2945-2964). */
 void gml_get_cnt_vec(int siz, int *cnt, int *vec, int *typ)
@@ -265,7 +283,7 @@ static void free_kernel(GmlSct *gml, GmlKrnSct *krn)
 void GmlStop(size_t GmlIdx)
 {
    int i;
-   GETGMLPTR(gml, GmlIdx);
+   GETGMLPTR_NOSETTLE(gml, GmlIdx);
 
    if(!gml)
       return;

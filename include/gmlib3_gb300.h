@@ -105,7 +105,10 @@ int      GmlxCompileKernelV   (size_t, const char *src, const char *name, int Ms
    or, for a large datatype on an idle instance whose device can address
    buf (pinned memory, or pageable memory where the device has pageable
    memory access), copies buf to the device and the mirror with one kernel
-   before returning.  Get is blocking. */
+   before returning.  Get is blocking; on the kernel path it writes buf
+   only, and the mirror is downloaded at the next call on the instance,
+   before that call reads the mirror or changes the device data (a Set of
+   the same datatype, which rewrites the mirror, skips the download). */
 int      GmlxSetData          (size_t, int DatIdx, const void *buf, size_t bytes);
 int      GmlxGetData          (size_t, int DatIdx, void *buf, size_t bytes);
 

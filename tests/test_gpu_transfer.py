@@ -61,8 +61,9 @@ def test_set_get_round_trip(G, direct, offset):
 
 def test_get_refreshes_the_mirror(G):
     """After a kernel changes the device data, GmlxGetData on either path
-    leaves the mirror equal to the downloaded data (as a download does)."""
-    n = 24
+    leaves the mirror equal to the downloaded data (as a download does).
+    48^3 hexes: 117,649 vertices, 1.9 MB, above the direct path's 1 MB."""
+    n = 48
     crd, tet, ref = G.cube_mesh(n, split=1, jitter=0.3, seed=3)
     res = []
     for direct in (True, False):
@@ -103,3 +104,43 @@ def test_new_mirrors_start_zeroed(G):
     finally:
         G.lib.GmlStop(g)
         G.lib.GmlStop(g2)
+
+
+def test_mirror_after_get_is_the_read_data(G):
+    """GmlxGetData on the direct path refreshes the host mirror at the next
+    call on the instance.  The mirror still holds the data of the read when
+    a kernel changes the device data before the line accessor looks (the
+    kernel's launch refreshes it first), and holds the new data when
+    GmlxSetData rewrites the datatype in between (1.9 MB of vertices, so
+    the transfers take the direct path)."""
+    n = 48
+    crd, tet, ref = G.cube_mesh(n, split=1, jitter=0.3, seed=4)
+    g = instance(G, True)
+    try:
+        v, t = G.upload_mesh(g, crd, tet, ref)
+        assert G.lib.GmlxMeshSetup(g, 1) == 1
+        assert G.lib.GmlxSmooth(g, 2, ctypes.c_float(1.0)) == 1
+        first = np.zeros_like(crd)
+        assert G.lib.GmlxGetData(g, v, first.ctypes.data, first.nbytes) == 1
+        # two reads in a row keep the same data
+        again = np.zeros_like(crd)
+        assert G.lib.GmlxGetData(g, v, again.ctypes.data, again.nbytes) == 1
+        assert np.array_equal(first, again)
+        # the sweeps change the device data; the mirror keeps the read
+        assert G.lib.GmlxSmooth(g, 2, ctypes.c_float(1.0)) == 1
+        now = np.zeros_like(crd)
+        assert G.lib.GmlxGetData(g, v, now.ctypes.data, now.nbytes) == 1
+        assert not np.array_equal(now, first)
+        assert G.lib.GmlxSmooth(g, 1, ctypes.c_float(1.0)) == 1
+        k = int(np.argmax(np.abs(now - first).sum(axis=1)))
+        assert line(G, g, v, k) == tuple(float(c) for c in now[k, :3])
+        # a read, then a whole rewrite: the mirror holds the rewrite
+        assert G.lib.GmlxGetData(g, v, now.ctypes.data, now.nbytes) == 1
+        new = np.ascontiguousarray(crd * np.float32(0.5))
+        assert G.lib.GmlxSetData(g, v, new.ctypes.data, new.nbytes) == 1
+        assert line(G, g, v, k) == tuple(float(c) for c in new[k, :3])
+        back = np.zeros_like(crd)
+        assert G.lib.GmlxGetData(g, v, back.ctypes.data, back.nbytes) == 1
+        assert np.array_equal(back, new)
+    finally:
+        G.lib.GmlStop(g)
