@@ -582,11 +582,9 @@ def other_configs(G, dev, dist):
                     "1e4..1e7 tets, reuse 0.5, 150 GB budget",
         "batching": {k: sv["batching"][k] for k in ("throughput_rps", "p50_ms", "p99_ms")},
         "serial_prefix": {k: sv["serial_prefix"][k] for k in ("throughput_rps", "p50_ms", "p99_ms")},
+        "capacity_saturated": {k: sv["capacity_saturated"][k]["throughput_rps"]
+                               for k in ("batching", "serial")},
         "capacity_saturated_ratio": sv["capacity_saturated"].get("batching_over_serial"),
-        "capacity_at_p99": {k: sv["capacity_at_p99"][k] for k in sv["capacity_at_p99"]
-                            if k != "batching" and k != "serial"} | {
-            "batching_max_rate": sv["capacity_at_p99"]["batching"]["max_rate_at_p99"],
-            "serial_max_rate": sv["capacity_at_p99"]["serial"]["max_rate_at_p99"]},
         "same_result_alone_and_in_mix": "%d of %d" % (sv["same"], sv["nser"])}
     ctypes.CDLL(None).fflush(None)
     return out
@@ -1235,12 +1233,12 @@ SERVE_SWEEP_RATES = (50, 100, 150, 200, 300, 400, 600)
 
 
 def serve_in_fresh_process(dev):
-    """Config 5 for the default line (10 s at 200 req/s, 4-s sweep runs),
-    measured by `bench.py --workload serve` in a process of its own: serve
+    """Config 5 for the default line (10 s at 200 req/s, no p99 sweep: its
+    4-s runs, dominated by target loads, swing from run to run), measured by `bench.py --workload serve` in a process of its own: serve
     runs that follow other heavy workloads in one process measure slower
     (host-side state), so the default line does not inherit the others'."""
     cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--workload", "serve",
-           "--duration", "10", "--sweep-seconds", "4"]
+           "--duration", "10", "--sweep-seconds", "0"]
     env = dict(os.environ, LOCAL_RANK=str(dev), RANK="0", WORLD_SIZE="1")
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, env=env)
     for line in r.stdout.splitlines():
