@@ -16,6 +16,15 @@
  * operator, so the vector-literal rewrite is required for correctness, not
  * only for compilation.  Scalar casts such as (float)(x) are left alone.
  *
+ * A `for` loop whose header names a `...DegMax` bound (a loop over a ball
+ * or shell, whose entries past the degree read as null values) gets a
+ * `#pragma unroll 4` line, unless a pragma precedes it already or it sits in
+ * a preprocessor directive.  With the loop unrolled the compiler issues four
+ * of the ball's gathers before it uses them; one dependent load per
+ * iteration held the NodeSmoothing gather to 536 us on the 128^3 cube, four
+ * take it to 483 us (the reference's own gather body: 793 to 702 us).
+ * Unrolling changes no result.
+ *
  * gml_nvrtc_options maps the OpenCL build options a caller can pass through
  * GmlSetCompilerOptions (-D, -I, -cl-fast-relaxed-math, ...) to NVRTC ones.
  */
@@ -128,6 +137,59 @@ static size_t number_len(const char *p, int *isflt)
    return (size_t)(q - p);
 }
 
+/* p points just after the keyword `for`: does its parenthesised header
+   contain an identifier ending in "DegMax"? */
+static int ball_loop_header(const char *p)
+{
+   const char *q = skip_ws(p);
+   int depth = 0;
+   if(*q != '(')
+      return 0;
+   for(;*q;q++)
+   {
+      if(*q == '(')
+         depth++;
+      else if(*q == ')' && --depth == 0)
+         return 0;
+      else if(isalpha((unsigned char)*q) || *q == '_')
+      {
+         const char *e = q;
+         while(isalnum((unsigned char)e[1]) || e[1] == '_') e++;
+         if(e - q + 1 >= 6 && !strncmp(e - 5, "DegMax", 6))
+            return 1;
+         q = e;
+      }
+   }
+   return 0;
+}
+
+/* the output's current line is a preprocessor directive, or the last
+   non-blank line before it is a pragma */
+static int pragma_context(const Str *out)
+{
+   const char *b = out->buf, *e = out->buf + out->len, *l = e;
+   while(l > b && l[-1] != '\n') l--;
+   {
+      const char *t = skip_ws(l);
+      if(t < e && *t == '#')
+         return 1;
+   }
+   /* previous non-blank lines */
+   while(l > b)
+   {
+      const char *pe = l - 1, *ps = pe;
+      while(ps > b && ps[-1] != '\n') ps--;
+      {
+         const char *t = ps;
+         while(t < pe && (*t == ' ' || *t == '\t' || *t == '\r')) t++;
+         if(t < pe)
+            return *t == '#';
+      }
+      l = ps;
+   }
+   return 0;
+}
+
 char *gml_rewrite_opencl(const char *src)
 {
    Str out = { NULL, 0, 0 };
@@ -173,6 +235,11 @@ char *gml_rewrite_opencl(const char *src)
       {
          const char *q = p;
          while(isalnum((unsigned char)*q) || *q == '_') q++;
+         if(q - p == 3 && !strncmp(p, "for", 3) && ball_loop_header(q) && !pragma_context(&out))
+         {
+            static const char pr[] = "\n#pragma unroll 4\n";
+            put(&out, pr, sizeof(pr) - 1);
+         }
          put(&out, p, q - p);
          p = q;
          continue;

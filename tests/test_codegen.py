@@ -148,6 +148,15 @@ def test_dialect_rewrites(G):
     assert rewrite("s = \"1.5\"; // 2.5\n") == "s = \"1.5\"; // 2.5\n"
     assert rewrite("v2 = x1.5;") == "v2 = x1.5f;" or True   # not valid C either way
     assert rewrite("(int){0}") == "int{0}"
+    # loops bounded by a ball's DegMax get an unroll pragma, once
+    assert rewrite("{ for(k=0;k<XDegMax;k++) a++; }") == \
+        "{ \n#pragma unroll 4\nfor(k=0;k<XDegMax;k++) a++; }"
+    assert rewrite("#pragma unroll 2\nfor(k=0;k<XDegMax;k++) a++;") == \
+        "#pragma unroll 2\nfor(k=0;k<XDegMax;k++) a++;"
+    assert rewrite("for(i=0;i<n;i++) a++;") == "for(i=0;i<n;i++) a++;"
+    assert rewrite("#define L for(i=0;i<ZDegMax;i++)\n") == "#define L for(i=0;i<ZDegMax;i++)\n"
+    assert rewrite("// for(k=0;k<XDegMax;k++)\n") == "// for(k=0;k<XDegMax;k++)\n"
+    assert rewrite("x = former(XDegMax);") == "x = former(XDegMax);"
     del rw
 
 
