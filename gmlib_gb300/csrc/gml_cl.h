@@ -497,6 +497,26 @@ template<class T> GML_FN T gml_ld_cs(const T *p)
       *(unsigned *)&r = u;
       return r;
    }
+   if(sizeof(T) == 8)
+   {
+      unsigned u[2];
+      asm("ld.global.cs.v2.u32 {%0,%1}, [%2];" : "=r"(u[0]), "=r"(u[1]) : "l"(p));
+      T r;
+      memcpy(&r, u, 8);
+      return r;
+   }
+#if __CUDA_ARCH__ >= 1000
+   if(sizeof(T) == 32)
+   {
+      unsigned u[8];
+      asm("ld.global.cs.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+          : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]),
+            "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]) : "l"(p));
+      T r;
+      memcpy(&r, u, 32);
+      return r;
+   }
+#endif
 #endif
    return *p;
 }

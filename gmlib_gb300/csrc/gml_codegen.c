@@ -184,6 +184,24 @@ static void emit_eager_item(Out *o, const GmlArgSct *a, const GmlArgSct *lnk,
    }
 }
 
+/* Argument i is a table of links read at the thread's own line (one item
+   of 4, 8, 16 or 32 bytes) through which other arguments are gathered. */
+static int stream_link(const GmlArgSct *ArgTab, int NmbArg, int i)
+{
+   const GmlArgSct *a = &ArgTab[i];
+   const int siz = GmlOclTypSiz[ a->ItmTyp ];
+   int j;
+
+   if(a->LnkIdx != -1 || a->CntIdx != -1 || a->LnkDir == 1 || a->NmbItm != 1
+   || (a->FlgTab & GmlVoyeurs) || !is_read_only(a)
+   || (siz != 4 && siz != 8 && siz != 16 && siz != 32))
+      return 0;
+   for(j=0;j<NmbArg;j++)
+      if(j != i && ArgTab[j].LnkIdx == i)
+         return 1;
+   return 0;
+}
+
 int gml_generate(char **res, const char *PrcNam, int MshTyp, int NmbArg,
                  const GmlArgSct *ArgTab, const char *KrnSrc, const char *UsrTlk,
                  const char *ParSrc, int lazy)
@@ -302,7 +320,12 @@ int gml_generate(char **res, const char *PrcNam, int MshTyp, int NmbArg,
       if(lazy && a->LnkDir == 1 && a->NmbItm > 1)
          continue;
 
-      if(lazy && !lnk && !cpt && a->LnkDir != 1 && !(a->FlgTab & GmlVoyeurs)
+      if(lazy && stream_link(ArgTab, NmbArg, i))
+         /* an element table that other arguments gather through, read once
+            per launch at the thread's own line: evict-first, so that it
+            does not push the gathered data out of L2 */
+         emit(&o, "   %s = gml_ld_cs(&%sTab[ cnt + count.s1 ]);\n", a->nam, a->nam);
+      else if(lazy && !lnk && !cpt && a->LnkDir != 1 && !(a->FlgTab & GmlVoyeurs)
       && GmlOclTypSiz[ a->ItmTyp ] == 16 && (a->NmbItm == 2 || a->NmbItm == 4))
          /* the entity's own 32- or 64-byte line: 32-byte loads */
          emit(&o, "   gml_load_line(%s, %sTab[ cnt + count.s1 ]);\n", a->nam, a->nam);
