@@ -9,6 +9,7 @@
 #include <string.h>
 #include <math.h>
 #include <pthread.h>
+#include <unistd.h>
 #include "gml_internal.h"
 #include "gmlib3_gb300.h"
 
