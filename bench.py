@@ -575,6 +575,11 @@ def other_configs(G, dev, dist):
                     for k, v in ns["kernels"].items()},
         "mean_quality_after": ns["q1"] / ns["nt"]}
     sv = serve_in_fresh_process(dev)
+    if sv is None:
+        out["serve_200rps"] = {"unavailable": "the serve run in its own process failed or "
+                                              "exceeded 600 s (its output is on stderr)"}
+        ctypes.CDLL(None).fflush(None)
+        return out
     out["serve_200rps"] = {
         "metric": "served requests/s (continuous batching), p50/p99 latency", "unit": "req/s",
         "value": sv["batching"]["throughput_rps"],
@@ -1240,7 +1245,11 @@ def serve_in_fresh_process(dev):
     cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--workload", "serve",
            "--duration", "10", "--sweep-seconds", "0"]
     env = dict(os.environ, LOCAL_RANK=str(dev), RANK="0", WORLD_SIZE="1")
-    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, env=env)
+    try:
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True,
+                           env=env, timeout=600)
+    except subprocess.TimeoutExpired:
+        return None
     for line in r.stdout.splitlines():
         if line.startswith("{"):
             d = json.loads(line)
@@ -1249,7 +1258,8 @@ def serve_in_fresh_process(dev):
                     "capacity_saturated": d["capacity_saturated"], "capacity_at_p99": c,
                     "same": int(d["same_result_alone_and_in_mix"].split()[0]),
                     "nser": int(d["same_result_alone_and_in_mix"].split()[-1])}
-    raise SystemExit("the serve run failed:\n" + r.stdout[-2000:] + r.stderr[-2000:])
+    sys.stderr.write("the serve run failed:\n" + r.stdout[-2000:] + r.stderr[-2000:] + "\n")
+    return None
 
 
 class ServePool:
