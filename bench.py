@@ -226,7 +226,10 @@ def workload_config(n, nv, nt, wset_mb, degrees=None):
             "per_sweep": "Jacobi sweep (boundary fixed) + quality, 64-bin histogram, "
                          "min/argmin, FP64 inverted flags",
             "jitter": JITTER, "seed": SEED, "omega": OMEGA,
-            "l2": "inputs larger than L2: %.0f MB working set > 129 MB L2" % wset_mb}
+            "l2": ("inputs larger than L2: %.0f MB working set > 129 MB L2" % wset_mb
+                   if wset_mb > 129 else
+                   "inputs fit in L2 (%.0f MB working set): a small case, not the "
+                   "benchmark configuration" % wset_mb)}
 
 
 # ---------------------------------------------------------------- CPU port
