@@ -461,6 +461,18 @@ int GmlxSetData(size_t GmlIdx, int DatIdx, const void *buf, size_t bytes)
    }
    drop_refresh(gml, dat);
    gml_wait_upload(gml, dat);
+   if(gml->MirOff)
+   {
+      /* an instance whose mirrors nobody reads: the device copy only, with
+         one kernel when the device can address buf, else by DMA */
+      if(!(gmd_host_addressable(gml->dev, buf) && gmd_fanout(gml->dev, buf, dat->GpuMem, NULL, bytes))
+      && !gmd_h2d_async(gml->dev, dat->GpuMem, buf, bytes))
+         return 0;
+      if(!gmd_sync(gml->dev))
+         return 0;
+      gml->MovSiz += bytes;
+      return 1;
+   }
    /* direct only when idle: the copy must land before the call returns (the
       caller may reuse buf), and waiting behind queued kernels would make an
       asynchronous upload blocking */

@@ -115,6 +115,9 @@ typedef struct
    int         Offline;               /* 1: no GPU, code generation only */
    int         Quiet;                 /* 1: no informational messages */
    int         PinOff;                /* 1: pageable host mirrors (no page locking) */
+   int         MirOff;                /* 1: whole-datatype sets write the device only and
+                                         the host mirrors are never read (the request
+                                         loop's own instances); mirrors stay pageable */
    char        **Names;               /* interned strings owned by the instance */
    int         NmbNames, CapNames;
    int         NmbMirOld;             /* datatypes whose MirOld is set */

@@ -17,6 +17,8 @@ int gmd_mesh_vt_csr(struct GmdCtx *ctx, const void *tet, int nt, int nv,
                     int *ptr, int *vt, int *tmp, int *err);
 int gmd_mesh_boundary(struct GmdCtx *ctx, const void *tet, int nt, const int *ptr,
                       const int *vt, int *fixed);
+/* fixed[v] = (ref[v] != 0), ref being the device copy of the vertex references */
+int gmd_mesh_fixed_from_ref(struct GmdCtx *ctx, const int *ref, int nv, int *fixed);
 /* ball of points as SELL-C-sigma: rows are vertices sorted by ball size in
    windows of `window` rows (32, 64, 128 or GML_SIGMA = 256; rowv packs
    (size << 26) | vertex), slices of 32 rows, rows padded to a multiple of 256 */

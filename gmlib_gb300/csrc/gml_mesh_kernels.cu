@@ -784,6 +784,23 @@ extern "C" int gmd_mesh_vt_csr(GmdCtx *ctx, const void *tet, int nt, int nv,
    return cudaGetLastError() == cudaSuccess;
 }
 
+/* fixed[v] = ref[v] != 0 */
+__global__ void fixed_from_ref_kernel(const int *__restrict__ ref, int nv, int *fixed)
+{
+   const int v = blockIdx.x * blockDim.x + threadIdx.x;
+   if(v < nv)
+      fixed[v] = ref[v] != 0;
+}
+
+extern "C" int gmd_mesh_fixed_from_ref(GmdCtx *ctx, const int *ref, int nv, int *fixed)
+{
+   cudaStream_t st = (cudaStream_t)gmd_stream(ctx);
+   if(nv <= 0)
+      return 1;
+   fixed_from_ref_kernel<<<nblk(nv, MK_THREADS), MK_THREADS, 0, st>>>(ref, nv, fixed);
+   return cudaGetLastError() == cudaSuccess;
+}
+
 extern "C" int gmd_mesh_boundary(GmdCtx *ctx, const void *tet, int nt, const int *ptr,
                                  const int *vt, int *fixed)
 {

@@ -134,17 +134,17 @@ int GmlxMeshSetup(size_t GmlIdx, int fix)
 
    if(fix == 1)
    {
-      /* vertices with a non-zero reference are fixed */
-      int *ref = (int *)gml->dat[ gml->RefIdx[ GmlVertices ] ].CpuMem, i;
-      int *fx = malloc((size_t)nv * sizeof(int));
-      if(!fx) { free_state(gml, n); return 0; }
-      gml_wait_upload(gml, &gml->dat[ gml->RefIdx[ GmlVertices ] ]);
-      for(i=0;i<nv;i++)
-         fx[i] = ref && ref[i] != 0;
+      /* vertices with a non-zero reference are fixed, read from the device
+         copy of the references (zero until set, as the host mirror), in
+         stream order after any upload of them */
+      const GmlDatSct *rd = gml->RefIdx[ GmlVertices ] ? &gml->dat[ gml->RefIdx[ GmlVertices ] ] : NULL;
       n->fixed = gmd_alloc(gml->dev, (size_t)nv * sizeof(int));
-      gmd_h2d_async(gml->dev, n->fixed, fx, (size_t)nv * sizeof(int));
-      gmd_sync(gml->dev);
-      free(fx);
+      if(!n->fixed || (rd && rd->GpuMem && rd->NmbLin >= nv
+                       && !gmd_mesh_fixed_from_ref(gml->dev, (const int *)rd->GpuMem, nv, n->fixed)))
+      {
+         free_state(gml, n);
+         return 0;
+      }
    }
    else if(fix == 2)
    {

@@ -227,8 +227,13 @@ static int load(SrvSct *s, SrvTarget *t)
    if(!g)
       return 0;
    GmlxSetTiming(g, 0);
-   /* no informational messages from served instances */
+   /* no informational messages from served instances; their whole-datatype
+      sets go to the device only and their host mirrors stay pageable and
+      untouched: nothing reads them, and page-locked mirrors cost the
+      pinning at every load and, at every eviction, a cudaFreeHost that
+      waits for all work on the device */
    ((GmlSct *)g)->Quiet = 1;
+   ((GmlSct *)g)->MirOff = 1;
    t->g = g;
    if(t->kind == 0)
    {

@@ -65,7 +65,7 @@ int gml_alloc_data(GmlSct *gml, GmlDatSct *dat)
 
    if(dat->MemAcs != GmlInternal)
    {
-      if(!gml->PinOff && dat->AloTyp != GmlArgDat && dat->MemSiz >= PIN_THRESHOLD
+      if(!gml->PinOff && !gml->MirOff && dat->AloTyp != GmlArgDat && dat->MemSiz >= PIN_THRESHOLD
       && (dat->CpuMem = gmd_host_alloc(dat->MemSiz)))
          dat->pinned = 1;
       else
