@@ -196,6 +196,43 @@ def traffic_for(kernel):
         return None
 
 
+def l1_wavefronts_for(kernel):
+    """L1 data-pipe wavefronts of one launch of a kernel (ncu
+    l1tex__data_pipe_lsu_wavefronts.sum) from the committed summary."""
+    path = os.path.join(ROOT, "profiles", "l1_wavefronts.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def sm_count(dev):
+    """Multiprocessor count of device `dev` from the CUDA driver."""
+    try:
+        cu = ctypes.CDLL("libcuda.so.1")
+        d, n = ctypes.c_int(), ctypes.c_int()
+        if cu.cuInit(0) or cu.cuDeviceGet(ctypes.byref(d), dev) \
+           or cu.cuDeviceGetAttribute(ctypes.byref(n), 16, d):      # MULTIPROCESSOR_COUNT
+            return None
+        return n.value
+    except OSError:
+        return None
+
+
+def l1_bound(kernel, launch_s, dev, clk):
+    """The kernel's L1 data-pipe load against its bound of one wavefront per
+    SM per cycle, at the SM clock sampled during the timed region."""
+    w, nsm = l1_wavefronts_for(kernel), sm_count(dev)
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    if not w or not nsm:
+        return None
+    return {"wavefronts_per_launch": w, "sms": nsm, "sm_mhz": mhz,
+            "bound_us": round(w / nsm / mhz, 2),
+            "frac": round(w / nsm / (mhz * 1e6) / launch_s, 4),
+            "source": "ncu l1tex__data_pipe_lsu_wavefronts.sum, profiles/l1_wavefronts.json"}
+
+
 def mesh(n):
     import gmlib_gb300 as G
     crd, tet, ref = G.cube_mesh(n, split=SPLIT, jitter=JITTER, seed=SEED)
@@ -433,11 +470,13 @@ def run_gpu(args, dist):
     achieved = kb / kt / 1e9
     roof = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
             "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic_for(name),
+            "l1_data_pipe": l1_bound(name, kt, dev, clk),
             "algorithmic_bytes_per_launch": kb, "mean_launch_us": round(kt * 1e6, 2),
             "peak_source": peak_src,
             "other_kernels": [{"kernel": k[0], "achieved": round(k[1] / k[2] / 1e9, 1),
                                "frac": round(k[1] / k[2] / 1e9 / peak, 4),
-                               "mean_launch_us": round(k[2] * 1e6, 2)} for k in kern[1:]]}
+                               "mean_launch_us": round(k[2] * 1e6, 2),
+                               "l1_data_pipe": l1_bound(k[0], k[2], dev, clk)} for k in kern[1:]]}
 
     # end to end through the C ABI with host buffers
     host_crd = np.ascontiguousarray(crd)
