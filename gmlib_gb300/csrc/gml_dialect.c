@@ -19,7 +19,7 @@
  * A `for` loop whose header names a `...DegMax` bound (a loop over a ball
  * or shell, whose entries past the degree read as null values) gets a
  * `#pragma unroll 4` line, unless a pragma precedes it already or it sits in
- * a preprocessor directive.  With the loop unrolled the compiler issues four
+ * a preprocessor directive (continuation lines included).  With the loop unrolled the compiler issues four
  * of the ball's gathers before it uses them; one dependent load per
  * iteration held the NodeSmoothing gather to 536 us on the 128^3 cube, four
  * take it to 483 us (the reference's own gather body: 793 to 702 us).
@@ -172,6 +172,15 @@ static int pragma_context(const Str *out)
    {
       const char *t = skip_ws(l);
       if(t < e && *t == '#')
+         return 1;
+   }
+   /* a continuation line (the line before ends with a backslash) belongs
+      to a directive or to a macro definition */
+   if(l > b)
+   {
+      const char *c = l - 1;                 /* the '\n' ending the previous line */
+      while(c > b && (c[-1] == '\r' || c[-1] == ' ' || c[-1] == '\t')) c--;
+      if(c > b && c[-1] == '\\')
          return 1;
    }
    /* previous non-blank lines */

@@ -155,6 +155,8 @@ def test_dialect_rewrites(G):
         "#pragma unroll 2\nfor(k=0;k<XDegMax;k++) a++;"
     assert rewrite("for(i=0;i<n;i++) a++;") == "for(i=0;i<n;i++) a++;"
     assert rewrite("#define L for(i=0;i<ZDegMax;i++)\n") == "#define L for(i=0;i<ZDegMax;i++)\n"
+    assert rewrite("#define S(x) \\\n   for(i=0;i<ZDegMax;i++) x;\n") == \
+        "#define S(x) \\\n   for(i=0;i<ZDegMax;i++) x;\n"
     assert rewrite("// for(k=0;k<XDegMax;k++)\n") == "// for(k=0;k<XDegMax;k++)\n"
     assert rewrite("x = former(XDegMax);") == "x = former(XDegMax);"
     del rw
