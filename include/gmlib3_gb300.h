@@ -195,7 +195,8 @@ typedef struct
 
 /* Build the topology the native kernels need (vertex->tet lists and the
    ball of points in SELL-32 form) on the GPU.  fix: 0 no vertex fixed,
-   1 vertices with a non-zero reference fixed, 2 vertices on the topological
+   1 vertices with a non-zero reference fixed (the device copy of the
+   references, as the kernels see them), 2 vertices on the topological
    boundary (faces owned by one tet) fixed.  Returns 1, or 0 on error (a ball
    of more than 64 points). */
 int      GmlxMeshSetup        (size_t, int fix);
