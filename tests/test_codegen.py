@@ -319,3 +319,38 @@ def test_triangle_ball_bodies_compile(G):
         assert k1 > 0 and k2 > 0
     finally:
         G.lib.GmlStop(g)
+
+
+def test_lines_and_streamed_links(G, offline):
+    """Lazy prologues read the element table through which the vertices are
+    gathered evict-first, read and write a datatype's own 32- or 64-byte
+    lines whole, and leave other lines item by item; the eager prologue
+    keeps the reference's per-item reads."""
+    g = offline
+    crd, tet, v, t = mesh(G, g)
+    opt = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 4, G.GmlFlt4, b"OptCrd")
+    tri = G.lib.GmlNewSolutionData(g, G.GmlTetrahedra, 3, G.GmlFlt4, b"Tri")
+    k = G.compile_kernel(g, body("optimal_points.cl"), "scatter", G.GmlTetrahedra,
+                         [(v, G.GmlReadMode, 0), (opt, G.GmlWriteMode, 0)])
+    assert k
+    s = source(G, g, k)
+    assert "TetVer = gml_ld_cs(&TetVerTab[ cnt + count.s1 ]);" in s
+    assert "VerCrd[0] =  VerCrdTab[ TetVer.s0 ]" in s
+    assert "gml_store_line(OptCrdTab[ cnt + count.s1 ], OptCrd);" in s
+    RW = G.GmlReadMode | G.GmlWriteMode
+    k2 = G.compile_kernel(g, b"{ Tri[0] = Tri[1] + Tri[2]; OptCrd[3] = OptCrd[0]; }", "lines",
+                          G.GmlTetrahedra, [(tri, RW, 0), (opt, RW, 0)])
+    assert k2
+    s2 = source(G, g, k2)
+    assert "gml_load_line(OptCrd, OptCrdTab[ cnt + count.s1 ]);" in s2
+    assert "gml_store_line(OptCrdTab[ cnt + count.s1 ], OptCrd);" in s2
+    # three items (48 bytes): item by item
+    assert "Tri[1] =  TriTab[ cnt + count.s1 ][1]" in s2
+    assert "TriTab[ cnt + count.s1 ][2] = Tri[2];" in s2
+    # eager prologue: the reference's text
+    G.lib.GmlxSetLazy(g, 0)
+    k3 = G.compile_kernel(g, b"{ Tri[0] = Tri[1] + Tri[2]; OptCrd[3] = OptCrd[0]; }", "lines_eager",
+                          G.GmlTetrahedra, [(tri, RW, 0), (opt, RW, 0)])
+    assert k3 and G.lib.GmlxKernelIsLazy(g, k3) == 0
+    s3 = source(G, g, k3)
+    assert "OptCrd[2] =  OptCrdTab[ cnt + count.s1 ][2]" in s3
